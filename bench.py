@@ -1,0 +1,313 @@
+#!/usr/bin/env python3
+"""Benchmark of the fused mass-spring step on one GB300 (or N replicas).
+
+Workload: the single large lattice -- 100^3 = 1,000,000 masses and
+12,731,796 springs (k log-uniform [1e3, 1e5], damping 0.1, 20% actuated),
+frictional plane and a fixed ball, dt = 1e-4 (titan_gb300.workloads.config2).
+A step is one time step of the whole lattice; its working set (~0.4-0.6 GB)
+is larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:      FP32-compensated fused step (headline), CUDA-graph replay, CUDA
+           events on the engine's stream; plus an FP64 drop-in figure, an
+           end-to-end figure through the C ABI with host buffers, and the
+           CPU oracle timed on the host cores.
+reference: the reference's per-spring / per-mass update functions restated
+           on the host (the CPU oracle, OpenMP with atomics as the reference's
+           kernels use) on all host threads, same workload and metric.
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "spring-updates/s"
+UNIT = "spring-updates/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="f32c", choices=["f32c", "f64", "f32"])
+    p.add_argument("--side", type=int, default=100)
+    p.add_argument("--fp64-steps", type=int, default=200)
+    p.add_argument("--e2e-chunk", type=int, default=100)
+    p.add_argument("--e2e-calls", type=int, default=5)
+    p.add_argument("--cpu-steps", type=int, default=8)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--tile", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(precision: str):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        return d.get(precision, {}).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for ln in getattr(self, "lines", []):
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_rate(sc, steps, threads):
+    from oracle import pyoracle as po
+    o = po.OracleSim(sc)
+    o.step(1, po.ATOMIC_OMP, threads)  # warm
+    t0 = time.perf_counter()
+    o.step(steps, po.ATOMIC_OMP, threads)
+    dt = time.perf_counter() - t0
+    return sc["left"].size * steps / dt, dt
+
+
+def run_ours(a, rank, world, local):
+    import numpy as np
+    import torch
+
+    import titan_gb300 as tg
+    from titan_gb300 import workloads as wl
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
+    sc = wl.config2(a.side)
+    ns, nm = sc["left"].size, sc["pos"].shape[0]
+    peak, peak_kind = peaks()
+
+    def timed(sim, steps):
+        stream = torch.cuda.ExternalStream(sim.stream, device=local)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(steps)
+        e1.record(stream)
+        sim.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        return e0.elapsed_time(e1)
+
+    sim = wl.make_sim(sc, prec, a.tile, device=local)
+    info = sim.plan_info()
+    sim.step(a.warmup)
+    sim.synchronize()
+    with ClockSampler(local) as clk:
+        ms = timed(sim, a.steps)
+    ms_max = max_over_ranks(ms)
+    st = sim.get_state(pos=True, vel=False)
+    finite = bool(np.all(np.isfinite(st["pos"])))
+    per_launch_s = ms / a.steps / 1e3
+    alg = info["algorithmic_bytes_per_step"]
+    achieved = alg / per_launch_s / 1e9
+    value = ns * a.steps * world / (ms_max / 1e3)
+    traffic = profiled_traffic(a.precision)
+
+    # end to end through the C ABI with host buffers
+    pos_h = np.ascontiguousarray(sc["pos"])
+    vel_h = np.zeros_like(pos_h)
+    out = {"pos": np.empty_like(pos_h)}
+    sim.set_mass_state(None, pos=pos_h, vel=vel_h)
+    sim.step(a.e2e_chunk)
+    sim.get_state(pos=True, vel=False, out=out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_calls):
+        sim.set_mass_state(None, pos=pos_h, vel=vel_h)
+        sim.step(a.e2e_chunk)
+        sim.get_state(pos=True, vel=False, out=out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    e2e_val = ns * a.e2e_chunk * a.e2e_calls * world / e2e_s
+    sim.close()
+
+    fp64 = None
+    if not a.no_fp64 and prec != tg.FP64:
+        s64 = wl.make_sim(sc, tg.FP64, 0, device=local)
+        i64 = s64.plan_info()
+        s64.step(3)
+        s64.synchronize()
+        ms64 = timed(s64, a.fp64_steps)
+        t = ms64 / a.fp64_steps / 1e3
+        fp64 = {"value": ns / t, "unit": UNIT, "ms_per_step": ms64 / a.fp64_steps, "steps": a.fp64_steps,
+                "mass_updates_per_s": nm / t, "algorithmic_gbs": i64["algorithmic_bytes_per_step"] / t / 1e9,
+                "note": "FP64 drop-in (bit-identical to the CPU oracle); FP64-ALU bound on GB300"}
+        s64.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, secs = cpu_oracle_rate(sc, a.cpu_steps, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{a.cpu_steps} full steps of the same 100^3 lattice, FP64, OpenMP with atomics "
+                         f"({secs:.1f} s wall)"}
+
+    if rank != 0:
+        return None
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": a.precision, "data": "synthetic (seeded lattice, BASELINE single-lattice configuration)",
+        "config": {"workload": f"single {a.side}^3 lattice, {nm} masses, {ns} springs, 20% actuated, "
+                               "plane + ball, dt=1e-4", "masses": nm, "springs": ns,
+                   "precision": a.precision, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "per-step working set larger than L2 (no flush)", "tiles": info["tiles"],
+                   "threads_per_cta": info["threads"], "smem_bytes": info["smem_bytes"]},
+        "mass_updates_per_s": nm * a.steps * world / (ms_max / 1e3),
+        "hbm_algorithmic_gbs": achieved,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
+                     "implementation_bytes_per_launch": info["implementation_bytes_per_step"],
+                     "kernel": "k_step (fused spring forces + mass update, one launch per step)"},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * nm * 8 / a.e2e_chunk,
+                "d2h_bytes_per_step": 3 * nm * 8 / a.e2e_chunk, "steps_per_call": a.e2e_chunk,
+                "calls": a.e2e_calls,
+                "path": "C ABI: set_mass_state(host pos+vel) -> step(chunk) -> get_state(host pos)"},
+        "gpu_launches": a.steps,
+        "clocks": clk.summary(),
+        "finite": finite,
+    }
+    if fp64:
+        res["fp64"] = fp64
+    if cpu:
+        res["cpu_baseline"] = cpu
+    return res
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return None
+    from titan_gb300 import workloads as wl
+    from oracle import pyoracle as po
+    sc = wl.config2(a.side)
+    ns = sc["left"].size
+    threads = os.cpu_count() or 1
+    o = po.OracleSim(sc)
+    o.step(min(a.warmup, 3), po.ATOMIC_OMP, threads)
+    k = max(1, min(a.steps, 60))
+    t0 = time.perf_counter()
+    o.step(k, po.ATOMIC_OMP, threads)
+    dt = time.perf_counter() - t0
+    val = ns * k / dt
+    return {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded lattice, BASELINE single-lattice configuration)",
+            "config": {"workload": f"single {a.side}^3 lattice, {sc['pos'].shape[0]} masses, {ns} springs, "
+                                   "20% actuated, plane + ball, dt=1e-4", "precision": "f64"},
+            "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{k} of the {a.steps} requested full steps (each the whole lattice), "
+                                       "reference per-spring/per-mass functions restated in C, OpenMP atomics"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        res = run_reference(a, rank, world)
+    else:
+        res = run_ours(a, rank, world, local)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

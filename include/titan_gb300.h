@@ -1,0 +1,244 @@
+/*
+ * titan_gb300.h -- C ABI of the GB300 mass-spring step engine.
+ *
+ * This is the drop-in boundary for the hot path of Titan's titan::Simulation
+ * (include/Titan/sim.h:37-220 in the reference).  The reference has no C ABI
+ * of its own: its boundary is the C++ class.  Each entry point below names
+ * the reference member function whose device-side work it replaces; the C++
+ * shim in include/Titan/sim.h (this repository) maps those member functions
+ * onto these calls one to one.
+ *
+ * Conventions
+ *   - Every call returns an int status (TITAN_GB300_OK == 0); no C++
+ *     exception crosses this boundary.  titan_gb300_last_error() gives the
+ *     message of the last failed call on that handle.
+ *   - Vectors are xyz-interleaved doubles: mass i's position is pos[3i..3i+2].
+ *   - Host buffers belong to the caller and are not retained after a call.
+ *   - Work is queued on the handle's own CUDA stream; calls that return data
+ *     to the host synchronise that stream first.
+ *   - Masses and springs are addressed by their index in the arrays the
+ *     caller uploaded (creation order in titan::Simulation).  Internally the
+ *     engine renumbers masses into spatial tiles; that order never leaks out.
+ */
+#ifndef TITAN_GB300_H
+#define TITAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TITAN_GB300_OK 0
+#define TITAN_GB300_EINVAL 1      /* bad argument or call order          */
+#define TITAN_GB300_ECUDA 2       /* CUDA runtime error                   */
+#define TITAN_GB300_ENOMEM 3      /* device or host allocation failed     */
+#define TITAN_GB300_ELIMIT 4      /* scene exceeds a documented limit     */
+#define TITAN_GB300_ESTATE 5      /* simulation ended / not started       */
+#define TITAN_GB300_ETIMEOUT 6    /* a bounded wait gave up               */
+#define TITAN_GB300_EBUDGET 7     /* serving admission over HBM budget    */
+
+/* Arithmetic of the step.  FP64 is the drop-in form (reference kernels are
+ * FP64).  FP32 runs positions/velocities in single precision.  FP32C runs the
+ * force arithmetic in FP32 and keeps positions and velocities as compensated
+ * (hi + lo) float pairs. */
+#define TITAN_GB300_FP64 0
+#define TITAN_GB300_FP32 1
+#define TITAN_GB300_FP32C 2
+
+/* Spring types: include/Titan/spring.h:17. */
+#define TITAN_GB300_PASSIVE_SOFT 0
+#define TITAN_GB300_PASSIVE_STIFF 1
+#define TITAN_GB300_ACTIVE_CONTRACT_THEN_EXPAND 2
+#define TITAN_GB300_ACTIVE_EXPAND_THEN_CONTRACT 3
+
+/* Local constraint types: include/Titan/object.h:223-225 (CONSTRAINT_TYPE). */
+#define TITAN_GB300_CONSTRAINT_PLANE 0
+#define TITAN_GB300_CONTACT_PLANE 1
+#define TITAN_GB300_BALL 2
+#define TITAN_GB300_DIRECTION 3
+
+typedef struct titan_gb300_sim titan_gb300_sim;
+
+/* ---- lifecycle --------------------------------------------------------- */
+
+/* Replaces Simulation::Simulation() (src/sim.cu:77-100): dt = 1e-4,
+ * g = (0, 0, -9.81).  device: CUDA ordinal; precision: TITAN_GB300_FP*. */
+int titan_gb300_create(titan_gb300_sim **out, int device, int precision);
+
+/* Replaces Simulation::~Simulation() / freeGPU() (src/sim.cu:131-221). */
+void titan_gb300_destroy(titan_gb300_sim *sim);
+
+/* Message of the last failed call on sim (never NULL). */
+const char *titan_gb300_last_error(const titan_gb300_sim *sim);
+
+/* ---- scene, host side (before start, or while paused) ------------------ */
+
+/* Replaces createMass (src/sim.cu:223-289) for a whole array of masses, plus
+ * Mass::setExternalForce / fix / setDrag (include/Titan/mass.h:27-38).
+ * vel, ext_force, fixed, drag may be NULL (zero / not fixed / no drag).  The
+ * drag coefficient is truncated to int as the reference's device struct does
+ * (include/Titan/object.h:213). */
+int titan_gb300_set_masses(titan_gb300_sim *sim, int64_t n, const double *pos,
+                           const double *vel, const double *m, const double *ext_force,
+                           const uint8_t *fixed, const double *drag);
+
+/* Replaces createSpring (src/sim.cu:291-341) for a whole array, with the
+ * actuation fields _type/_omega/_damping (include/Titan/spring.h:49-55).
+ * left/right = -1 means no mass attached (the reference then skips the spring,
+ * src/sim.cu:1052).  type, omega may be NULL (passive).  amp and phase extend
+ * the reference's fixed 0.2 sin(omega t) actuation: NULL means amp = 0.2,
+ * phase = 0, which reproduces the reference exactly. */
+int titan_gb300_set_springs(titan_gb300_sim *sim, int64_t n, const int32_t *left,
+                            const int32_t *right, const double *k, const double *rest,
+                            const double *damping, const int32_t *type, const double *omega,
+                            const double *amp, const double *phase);
+
+/* Replaces Mass::addConstraint (src/mass.cu:78-101) for all masses at once:
+ * records of mass i are mass_ptr[i] .. mass_ptr[i+1]-1 (mass_ptr has n+1
+ * entries), vec/num as given to addConstraint (normalised here as the
+ * reference constructors do).  Records are applied in the reference's order:
+ * contact planes, balls, constraint planes, directions (src/sim.cu:1117-1131). */
+int titan_gb300_set_local_constraints(titan_gb300_sim *sim, const int64_t *mass_ptr,
+                                      const int32_t *type, const double *vec, const double *num);
+
+/* Replaces createPlane (src/sim.cu:1998-2023); normal is normalised. */
+int titan_gb300_add_plane(titan_gb300_sim *sim, const double normal[3], double offset,
+                          double friction_k, double friction_s);
+
+/* Replaces createBall (src/sim.cu:2025-2035). */
+int titan_gb300_add_ball(titan_gb300_sim *sim, const double center[3], double radius);
+
+/* Replaces clearConstraints (src/sim.cu:2037-2040): removes global planes and balls. */
+int titan_gb300_clear_constraints(titan_gb300_sim *sim);
+
+/* Replaces setTimeStep (src/sim.cu:797-807); dt <= 0 is EINVAL. */
+int titan_gb300_set_time_step(titan_gb300_sim *sim, double dt);
+double titan_gb300_get_time_step(const titan_gb300_sim *sim);
+
+/* Replaces setGlobalAcceleration (src/sim.cu:2081-2087). */
+int titan_gb300_set_global_acc(titan_gb300_sim *sim, const double g[3]);
+
+/* Groups masses into independent bodies: body b owns masses
+ * mass_ptr[b] .. mass_ptr[b+1]-1 (creation order, contiguous).  Tiles never
+ * straddle two bodies.  Optional; without it the scene is one body. */
+int titan_gb300_set_bodies(titan_gb300_sim *sim, int64_t nbodies, const int64_t *mass_ptr);
+
+/* Per-body ground plane (a contact plane with friction that acts only on the
+ * masses of that body).  normal is normalised. */
+int titan_gb300_set_body_plane(titan_gb300_sim *sim, int64_t body, const double normal[3],
+                               double offset, double friction_k, double friction_s);
+
+/* ---- device side -------------------------------------------------------- */
+
+/* Replaces start() (src/sim.cu:1349-1390) minus the thread spawn: builds the
+ * tile plan (spatial renumbering, spring slabs, per-mass incidence), uploads
+ * the structure-of-arrays state and resets time to 0.  tile_masses = 0 picks
+ * the tuned default. */
+int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
+
+/* One iteration of the reference's execute() loop body (src/sim.cu:1569-1590)
+ * nsteps times: spring forces + mass update fused into one kernel per step,
+ * replayed from cached CUDA graphs.  Asynchronous. */
+int titan_gb300_step(titan_gb300_sim *sim, int64_t nsteps);
+
+/* Wait for queued work; replaces the cudaDeviceSynchronize at src/sim.cu:1570. */
+int titan_gb300_synchronize(titan_gb300_sim *sim);
+
+/* Replaces time() (src/sim.cu:1082): host-accumulated T (T += dt per step). */
+double titan_gb300_time(const titan_gb300_sim *sim);
+
+/* Number of steps run since start(). */
+int64_t titan_gb300_steps(const titan_gb300_sim *sim);
+
+/* Sets T (the time the next step's actuation sees).  The reference sets T = 0
+ * in start() (src/sim.cu:1369); this lets a host rebuild a scene mid-run
+ * (topology edited while paused) and continue at the same time. */
+int titan_gb300_set_time(titan_gb300_sim *sim, double T);
+
+/* Replaces getAll() / massFromArray (src/sim.cu:642-653, 983-1005): copies
+ * pos, vel, acc (3n each) and per-mass local time T (n) back in creation
+ * order.  Any pointer may be NULL. */
+int titan_gb300_get_state(titan_gb300_sim *sim, double *pos, double *vel, double *acc,
+                          double *T);
+
+/* get(Mass*) (src/sim.cu:588-601) for a list of masses. */
+int titan_gb300_get_masses(titan_gb300_sim *sim, int64_t count, const int64_t *idx,
+                           double *pos, double *vel, double *acc, double *T);
+
+/* Replaces setAll() / set(Mass*) / set(Container*) (src/sim.cu:603-615,
+ * 655-766) for masses: overwrites pos, vel, m, extern force, fixed, drag and
+ * local time of the listed masses (idx == NULL: all n, in order).  Any data
+ * pointer may be NULL to leave that field unchanged.  Forces restart at 0. */
+int titan_gb300_set_mass_state(titan_gb300_sim *sim, int64_t count, const int64_t *idx,
+                               const double *pos, const double *vel, const double *m,
+                               const double *ext_force, const uint8_t *fixed,
+                               const double *drag, const double *T);
+
+/* Replaces set(Spring*) / the spring half of setAll() (src/sim.cu:632-640,
+ * 746-764): new k, rest, damping, type, omega (and the amp/phase extension)
+ * for the listed springs (idx == NULL: all).  Endpoints cannot change here.
+ * NULL leaves a field unchanged. */
+int titan_gb300_set_spring_params(titan_gb300_sim *sim, int64_t count, const int64_t *idx,
+                                  const double *k, const double *rest, const double *damping,
+                                  const int32_t *type, const double *omega, const double *amp,
+                                  const double *phase);
+
+/* FP64 diagnostics on the device, following test/testutil/utils.h:12-43:
+ * energy[4] = {spring PE, kinetic, gravity PE (g_mag * z * m), total};
+ * momentum[6] = {linear xyz, angular xyz} with angular = sum cross(m v, x).
+ * Either output may be NULL.  Deterministic (fixed-order two-pass reduction). */
+int titan_gb300_diagnostics(titan_gb300_sim *sim, double g_mag, double energy[4],
+                            double momentum[6]);
+
+/* CUDA stream (cudaStream_t) the handle queues work on. */
+void *titan_gb300_stream(titan_gb300_sim *sim);
+
+/* Plan figures for reports: out[0] masses, [1] springs, [2] tiles,
+ * [3] slab entries, [4] halo slots, [5] incidence words, [6] heavy masses,
+ * [7] dynamic shared memory bytes per CTA, [8] threads per CTA,
+ * [9] algorithmic bytes per step, [10] implementation bytes per step
+ * (tables and slabs as laid out), [11] actuated entries. */
+int titan_gb300_plan_info(const titan_gb300_sim *sim, int64_t out[12]);
+
+/* ---- host-only helpers (no GPU needed) ------------------------------------ */
+
+/* Builds the tile plan of the current scene on the host only (no CUDA call),
+ * for inspection and validation; start() builds its own.  The tables are
+ * copied out with titan_gb300_plan_table, which returns the element count
+ * (and copies when out != NULL), or -1 for an unknown table. */
+int titan_gb300_plan_host(titan_gb300_sim *sim, int tile_masses);
+int64_t titan_gb300_plan_table(const titan_gb300_sim *sim, int table, void *out);
+#define TITAN_GB300_T_NEW2OLD 0        /* int32: tiled index -> creation index   */
+#define TITAN_GB300_T_TILE_MASS_OFF 1  /* int64: ntiles+1                        */
+#define TITAN_GB300_T_TILE_HALO_OFF 2  /* int64: ntiles+1                        */
+#define TITAN_GB300_T_HALO 3           /* int32: tiled indices of halo masses    */
+#define TITAN_GB300_T_TILE_ENT_OFF 4   /* int64: ntiles+1                        */
+#define TITAN_GB300_T_TILE_NACT 5      /* int32: actuated entries lead each slab */
+#define TITAN_GB300_T_ENT_ENDS 6       /* uint32: left slot | right << 12 | type << 24 */
+#define TITAN_GB300_T_ENT_SPRING 7     /* int64: spring of each entry            */
+#define TITAN_GB300_T_TILE_WARP_OFF 8  /* int64: ntiles+1                        */
+#define TITAN_GB300_T_WARP_INC_OFF 9   /* uint32: per warp, into INC             */
+#define TITAN_GB300_T_DEG 10           /* uint8: per tiled mass, 255 = heavy     */
+#define TITAN_GB300_T_INC 11           /* uint16: entry | 0x8000 for a left end  */
+#define TITAN_GB300_T_TILE_HEAVY_OFF 12 /* int64: ntiles+1                       */
+#define TITAN_GB300_T_HEAVY_LOCAL 13   /* uint16                                 */
+#define TITAN_GB300_T_HEAVY_INC_OFF 14 /* uint32: nheavy+1                       */
+#define TITAN_GB300_T_HEAVY_INC 15     /* uint16                                 */
+#define TITAN_GB300_T_BODY_OF_TILE 16  /* int32                                  */
+
+/* Lattice builder of createLattice (src/sim.cu:1923-1944, src/object.cu:232-293):
+ * fills pos (3*nx*ny*nz) and, when non-NULL, left/right/rest of the
+ * titan_gb300_lattice_springs(nx,ny,nz) springs, in the reference's order. */
+int64_t titan_gb300_lattice_springs(int nx, int ny, int nz);
+int titan_gb300_lattice(const double center[3], const double dims[3], int nx, int ny, int nz,
+                        double *pos, int32_t *left, int32_t *right, double *rest);
+
+/* Version string of this library. */
+const char *titan_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,191 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry point
+include/titan_gb300.h declares, and the host tile plan satisfies every
+invariant the step kernel relies on."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import titan_gb300 as tg
+from titan_gb300 import workloads as wl
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "titan_gb300.h").read_text()
+    return sorted(set(re.findall(r"\b(titan_gb300_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = ctypes.CDLL(str(tg.library_path()))
+    syms = declared_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_version_and_host_helpers():
+    assert b"sm_103a" in tg.lib().titan_gb300_version()
+    assert tg.lattice_springs(5, 5, 5) == 1036
+
+
+def test_create_needs_no_gpu_and_validates():
+    s = tg.Sim(tg.FP64)
+    with pytest.raises(tg.TitanError):
+        s.set_time_step(0.0)
+    with pytest.raises(tg.TitanError):
+        s.step(1)  # not started
+    s.close()
+
+
+# ------------------------------------------------------- plan validation ---
+T = {name: i for i, name in enumerate(
+    ["new2old", "tile_mass_off", "tile_halo_off", "halo", "tile_ent_off", "tile_nact", "ent_ends", "ent_spring",
+     "tile_warp_off", "warp_inc_off", "deg", "inc", "tile_heavy_off", "heavy_local", "heavy_inc_off", "heavy_inc",
+     "body_of_tile"])}
+DT = {"new2old": np.int32, "tile_mass_off": np.int64, "tile_halo_off": np.int64, "halo": np.int32,
+      "tile_ent_off": np.int64, "tile_nact": np.int32, "ent_ends": np.uint32, "ent_spring": np.int64,
+      "tile_warp_off": np.int64, "warp_inc_off": np.uint32, "deg": np.uint8, "inc": np.uint16,
+      "tile_heavy_off": np.int64, "heavy_local": np.uint16, "heavy_inc_off": np.uint32, "heavy_inc": np.uint16,
+      "body_of_tile": np.int32}
+
+
+def plan_tables(sc, tile, precision=tg.FP32C):
+    s = tg.Sim(precision)
+    wl.load(s, sc, start=False)
+    rc = s._L.titan_gb300_plan_host(s._h, tile)
+    s._check(rc, "plan_host")
+    out = {}
+    for name, idx in T.items():
+        n = s._L.titan_gb300_plan_table(s._h, idx, None)
+        a = np.zeros(max(n, 0), DT[name])
+        s._L.titan_gb300_plan_table(s._h, idx, a.ctypes.data_as(ctypes.c_void_p))
+        out[name] = a
+    s.close()
+    return out
+
+
+def validate(sc, P, heavy_threshold=96):
+    n = sc["pos"].shape[0]
+    left, right = sc["left"], sc["right"]
+    ns = left.size
+    fixed = sc.get("fixed")
+    fixed = np.zeros(n, bool) if fixed is None else np.asarray(fixed, bool)
+    typ = sc.get("type")
+    new2old = P["new2old"]
+    assert sorted(new2old.tolist()) == list(range(n))
+    old2new = np.empty(n, np.int64)
+    old2new[new2old] = np.arange(n)
+    tmo = P["tile_mass_off"]
+    ntiles = tmo.size - 1
+    tile_of = np.empty(n, np.int64)
+    for t in range(ntiles):
+        tile_of[tmo[t]:tmo[t + 1]] = t
+    if "body_ptr" in sc:
+        bp = sc["body_ptr"]
+        body_of_old = np.searchsorted(bp, np.arange(n), side="right") - 1
+        for t in range(ntiles):
+            bodies = set(body_of_old[new2old[tmo[t]:tmo[t + 1]]].tolist())
+            assert bodies == {P["body_of_tile"][t]}
+    valid = (left >= 0) & (right >= 0) & (left < n) & (right < n)
+    # expected incidence per new mass: ascending springs, right before left
+    expect = [[] for _ in range(n)]
+    for s in range(ns):
+        if not valid[s]:
+            continue
+        r, l = old2new[right[s]], old2new[left[s]]
+        if not fixed[right[s]]:
+            expect[r].append((s, 1))
+        if not fixed[left[s]]:
+            expect[l].append((s, -1))
+    seen_in_tile = {}
+    heavy_seen = 0
+    for t in range(ntiles):
+        m0, m1 = tmo[t], tmo[t + 1]
+        nm = m1 - m0
+        halo = P["halo"][P["tile_halo_off"][t]:P["tile_halo_off"][t + 1]]
+        assert np.all(np.diff(halo) > 0)
+        assert not np.any((halo >= m0) & (halo < m1))
+        slot2g = np.concatenate([np.arange(m0, m1), halo])
+        e0, e1 = P["tile_ent_off"][t], P["tile_ent_off"][t + 1]
+        ends = P["ent_ends"][e0:e1]
+        sp = P["ent_spring"][e0:e1]
+        nact = P["tile_nact"][t]
+        if typ is not None:
+            assert np.all(np.isin(typ[sp[:nact]], [2, 3])) and not np.any(np.isin(typ[sp[nact:]], [2, 3]))
+        a, b, ty = ends & 0xFFF, (ends >> 12) & 0xFFF, (ends >> 24) & 3
+        assert np.all(a < nm + halo.size) and np.all(b < nm + halo.size)
+        assert np.array_equal(new2old[slot2g[a]], left[sp])
+        assert np.array_equal(new2old[slot2g[b]], right[sp])
+        if typ is not None:
+            assert np.array_equal(ty, typ[sp] & 3)
+        remote = set(slot2g[a][a >= nm].tolist()) | set(slot2g[b][b >= nm].tolist())
+        assert remote == set(halo.tolist())
+        for s in sp.tolist():
+            seen_in_tile.setdefault(s, set()).add(t)
+        # incidence
+        w0 = P["tile_warp_off"][t]
+        hl = P["heavy_local"][P["tile_heavy_off"][t]:P["tile_heavy_off"][t + 1]].tolist()
+        for i in range(nm):
+            g = m0 + i
+            d = int(P["deg"][g])
+            if d == 255:
+                h = P["tile_heavy_off"][t] + hl.index(i)
+                codes = P["heavy_inc"][P["heavy_inc_off"][h]:P["heavy_inc_off"][h + 1]]
+                heavy_seen += 1
+                assert len(expect[g]) > heavy_threshold
+            else:
+                off = int(P["warp_inc_off"][w0 + i // 32])
+                codes = P["inc"][off + (i % 32) + 32 * np.arange(d)]
+            got = [(int(sp[c & 0x7FFF]), -1 if c & 0x8000 else 1) for c in codes.tolist()]
+            assert got == expect[g], (t, i)
+    assert heavy_seen == sum(1 for e in expect if len(e) > heavy_threshold)
+    # each valid spring with a free end sits in the tile of every free end
+    for s in range(ns):
+        if not valid[s]:
+            continue
+        want = {tile_of[old2new[x]] for x in (left[s], right[s]) if not fixed[x]}
+        assert seen_in_tile.get(s, set()) == want, s
+
+
+@pytest.mark.parametrize("tile", [32, 64, 512])
+def test_plan_lattice(tile):
+    sc = wl.lattice_scene((0, 0, 1), (1, 1, 1), 9, 7, 8)
+    validate(sc, plan_tables(sc, tile))
+
+
+def test_plan_actuated_fixed_and_loops():
+    rng = np.random.default_rng(2)
+    sc = wl.lattice_scene((0, 0, 1), (1, 1, 1), 6, 6, 6)
+    wl.actuate(sc, rng, 0.3, 0.1)
+    sc["fixed"] = (rng.random(216) < 0.1).astype(np.uint8)
+    # a self-loop, a dangling spring and a duplicate
+    sc["left"] = np.concatenate([sc["left"], [5, -1, 3]]).astype(np.int32)
+    sc["right"] = np.concatenate([sc["right"], [5, 7, 4]]).astype(np.int32)
+    for key, val in (("k", 1e3), ("rest", 0.1), ("damping", 0.0), ("omega", 0.0), ("amp", 0.2), ("phase", 0.0)):
+        sc[key] = np.concatenate([sc[key], [val] * 3])
+    sc["type"] = np.concatenate([sc["type"], [0, 0, 0]]).astype(np.int32)
+    validate(sc, plan_tables(sc, 64))
+
+
+def test_plan_heavy_hub():
+    from tests.test_oracle import hub_scene
+    sc = hub_scene(degree=300)
+    validate(sc, plan_tables(sc, 64))
+
+
+def test_plan_bodies():
+    sc = wl.config3(nbodies=12, seed=4, side_range=(3, 6))
+    validate(sc, plan_tables(sc, 64))
+
+
+def test_plan_rejects_hub_beyond_slab():
+    n = 40000
+    sc = {"pos": np.random.default_rng(0).normal(size=(n, 3)), "m": np.full(n, 0.1),
+          "left": np.zeros(n - 1, np.int32), "right": np.arange(1, n, dtype=np.int32),
+          "k": np.ones(n - 1), "rest": np.ones(n - 1), "planes": [], "balls": [], "g": np.zeros(3), "dt": 1e-4}
+    with pytest.raises(tg.TitanError, match="ELIMIT"):
+        plan_tables(sc, 64)

@@ -1,0 +1,1080 @@
+// capi.cu -- the C ABI of include/titan_gb300.h.
+//
+// Replaces the reference's device-state layer and run loop
+// (src/sim.cu:821-1017 AoS per-object cudaMalloc + pointer arrays, and
+// src/sim.cu:1503-1617 sync + two launches per step) with: one tile plan,
+// structure-of-arrays buffers allocated once, and CUDA-graph replay of the
+// fused step kernel on a private stream.
+#include "titan_gb300.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "engine.h"
+#include "plan.h"
+
+using tg::P_FP32;
+using tg::P_FP32C;
+using tg::P_FP64;
+
+namespace {
+
+constexpr int kChunk = 64;  // steps per cached graph
+
+double norm3(const double *v) {
+    double a = v[0] * v[0], b = v[1] * v[1], c = v[2] * v[2];
+    return std::sqrt((a + b) + c);
+}
+
+struct DevMem {
+    std::vector<void *> ptrs;
+    void *get(size_t bytes, cudaError_t &e) {
+        void *p = nullptr;
+        if (bytes == 0) bytes = 16;
+        e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) ptrs.push_back(p);
+        return p;
+    }
+    void release() {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+}  // namespace
+
+struct titan_gb300_sim {
+    int device = 0, prec = P_FP64;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // host scene (creation order)
+    int64_t n = 0;
+    std::vector<double> pos, vel, m, ext, drag_in;
+    std::vector<uint8_t> fixed;
+    std::vector<int32_t> drag;
+    std::vector<int64_t> lc_ptr;  // n+1 or empty
+    std::vector<int32_t> lc_type;
+    std::vector<double> lc_rec;   // 4 per record
+    int64_t ns = 0;
+    std::vector<int32_t> left, right, type;
+    std::vector<double> k, rest, damping, omega, amp, phase;
+    std::vector<std::array<double, 6>> planes;
+    std::vector<std::array<double, 4>> balls;
+    std::vector<int64_t> body_ptr;
+    std::vector<std::array<double, 6>> body_plane;
+    std::vector<uint8_t> body_has_plane;
+    double dt = 1e-4;
+    double g[3] = {0.0, 0.0, -9.81};
+
+    // run state
+    bool started = false;
+    double T = 0.0;
+    int64_t steps = 0;
+    int parity = 0;
+    std::vector<double> mT0;       // per-mass local time at its last upload
+    std::vector<int64_t> mTstep;   // step count at that upload
+    std::vector<std::pair<int64_t, double>> dt_log;  // (first step, dt)
+
+    // device
+    tg::Plan plan;
+    DevMem mem;
+    tg::StepArgs args{};
+    tg::DevParams hprm{};
+    tg::DevParams *dprm = nullptr;
+    int threads = 512;
+    int tile_masses = 0;
+    size_t smem = 0;
+    int64_t npad = 0;
+    int32_t *d_old2new = nullptr;
+    double *d_xfer = nullptr;     // 9n doubles
+    int64_t *d_idx = nullptr;     // n
+    double *h_xfer = nullptr;     // pinned 9n doubles
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;
+    // diagnostics (lazy)
+    int32_t *d_sl = nullptr, *d_sr = nullptr;
+    double *d_sk = nullptr, *d_srest = nullptr, *d_partials = nullptr, *d_dout = nullptr;
+
+    size_t rsize() const { return prec == P_FP64 ? sizeof(double) : sizeof(float); }
+    int comps() const { return prec == P_FP32C ? 12 : 6; }
+
+    int fail(int code, const std::string &msg) {
+        err = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what) {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        return TITAN_GB300_ECUDA;
+    }
+
+    void drop_graphs() {
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+    void free_device() {
+        drop_graphs();
+        mem.release();
+        if (h_xfer) cudaFreeHost(h_xfer);
+        h_xfer = nullptr;
+        d_sl = d_sr = nullptr;
+        d_sk = d_srest = d_partials = d_dout = nullptr;
+    }
+    ~titan_gb300_sim() {
+        if (stream) cudaStreamSynchronize(stream);
+        free_device();
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return s->cuda_fail(e_, what); \
+    } while (0)
+
+uint8_t mass_flags(const titan_gb300_sim *s, int64_t i) {
+    uint8_t f = 0;
+    if (!s->fixed.empty() && s->fixed[i]) f |= tg::MF_FIXED;
+    if (!s->ext.empty() && (s->ext[3 * i] != 0.0 || s->ext[3 * i + 1] != 0.0 || s->ext[3 * i + 2] != 0.0))
+        f |= tg::MF_EXT;
+    if (!s->drag.empty() && s->drag[i] != 0) f |= tg::MF_DRAG;
+    if (!s->lc_ptr.empty() && s->lc_ptr[i + 1] > s->lc_ptr[i]) f |= tg::MF_LOCAL;
+    return f;
+}
+
+void fill_params(titan_gb300_sim *s) {
+    tg::DevParams &p = s->hprm;
+    std::memset(&p, 0, sizeof(p));
+    p.dt = s->dt;
+    p.dt_hi = (float)s->dt;
+    p.dt_lo = (float)(s->dt - (double)p.dt_hi);
+    for (int c = 0; c < 3; c++) {
+        p.g[c] = s->g[c];
+        p.gf[c] = (float)s->g[c];
+    }
+    p.nplanes = (int32_t)s->planes.size();
+    p.nballs = (int32_t)s->balls.size();
+    for (size_t j = 0; j < s->planes.size(); j++)
+        for (int c = 0; c < 6; c++) {
+            p.plane[j][c] = s->planes[j][c];
+            p.planef[j][c] = (float)s->planes[j][c];
+        }
+    for (size_t j = 0; j < s->balls.size(); j++)
+        for (int c = 0; c < 4; c++) {
+            p.ball[j][c] = s->balls[j][c];
+            p.ballf[j][c] = (float)s->balls[j][c];
+        }
+}
+
+int upload_params(titan_gb300_sim *s) {
+    fill_params(s);
+    CK(cudaMemcpyAsync(s->dprm, &s->hprm, sizeof(tg::DevParams), cudaMemcpyHostToDevice, s->stream),
+       "upload params");
+    CK(cudaMemcpyAsync(s->args.tbuf + s->parity, &s->T, sizeof(double), cudaMemcpyHostToDevice, s->stream),
+       "upload time");
+    CK(cudaStreamSynchronize(s->stream), "upload params");
+    return TITAN_GB300_OK;
+}
+
+template <typename R>
+std::vector<R> to_real(const std::vector<double> &v) {
+    return std::vector<R>(v.begin(), v.end());
+}
+
+// Per-mass device arrays (m, flags, ext, drag, local constraints) from the
+// host mirror, in tiled order.
+int upload_mass_attrs(titan_gb300_sim *s) {
+    const tg::Plan &P = s->plan;
+    const int64_t n = s->n, np = s->npad;
+    std::vector<uint8_t> flags(np, tg::MF_FIXED);
+    std::vector<double> md(np, 1.0), extd(3 * np, 0.0);
+    std::vector<int32_t> dragn(np, 0), lcp(np + 1, 0);
+    std::vector<int32_t> lct;
+    std::vector<double> lcr;
+    for (int64_t g = 0; g < n; g++) {
+        int64_t i = P.new2old[g];
+        uint8_t f = mass_flags(s, i);
+        int32_t b = 0;
+        if (!s->body_ptr.empty())
+            b = (int32_t)(std::upper_bound(s->body_ptr.begin(), s->body_ptr.end(), i) - s->body_ptr.begin() - 1);
+        if (!s->body_has_plane.empty() && s->body_has_plane[b]) f |= tg::MF_BODYPLANE;
+        flags[g] = f;
+        md[g] = s->m[i];
+        if (!s->ext.empty())
+            for (int c = 0; c < 3; c++) extd[c * np + g] = s->ext[3 * i + c];
+        if (!s->drag.empty()) dragn[g] = s->drag[i];
+        lcp[g] = (int32_t)lct.size();
+        if (!s->lc_ptr.empty())
+            for (int64_t r = s->lc_ptr[i]; r < s->lc_ptr[i + 1]; r++) {
+                lct.push_back(s->lc_type[r]);
+                for (int c = 0; c < 4; c++) lcr.push_back(s->lc_rec[4 * r + c]);
+            }
+    }
+    for (int64_t g = n; g <= np; g++) lcp[g] = (int32_t)lct.size();
+    auto &a = s->args;
+    CK(cudaMemcpy(const_cast<uint8_t *>(a.flags), flags.data(), np, cudaMemcpyHostToDevice), "upload flags");
+    if (s->prec == P_FP64) {
+        CK(cudaMemcpy(const_cast<void *>(a.mass), md.data(), np * 8, cudaMemcpyHostToDevice), "upload m");
+        CK(cudaMemcpy(const_cast<void *>(a.ext), extd.data(), 3 * np * 8, cudaMemcpyHostToDevice), "upload ext");
+    } else {
+        auto mf = to_real<float>(md);
+        auto ef = to_real<float>(extd);
+        CK(cudaMemcpy(const_cast<void *>(a.mass), mf.data(), np * 4, cudaMemcpyHostToDevice), "upload m");
+        CK(cudaMemcpy(const_cast<void *>(a.ext), ef.data(), 3 * np * 4, cudaMemcpyHostToDevice), "upload ext");
+    }
+    CK(cudaMemcpy(const_cast<int32_t *>(a.drag), dragn.data(), np * 4, cudaMemcpyHostToDevice), "upload drag");
+    CK(cudaMemcpy(const_cast<int32_t *>(a.lc_ptr), lcp.data(), (np + 1) * 4, cudaMemcpyHostToDevice), "upload lc");
+    if (!lct.empty()) {
+        cudaError_t e;
+        int32_t *t = (int32_t *)s->mem.get(lct.size() * 4, e);
+        if (!t) return s->cuda_fail(e, "alloc lc");
+        double *r = (double *)s->mem.get(lcr.size() * 8, e);
+        if (!r) return s->cuda_fail(e, "alloc lc");
+        CK(cudaMemcpy(t, lct.data(), lct.size() * 4, cudaMemcpyHostToDevice), "upload lc");
+        CK(cudaMemcpy(r, lcr.data(), lcr.size() * 8, cudaMemcpyHostToDevice), "upload lc");
+        a.lc_type = t;
+        a.lc_rec = r;
+    }
+    return TITAN_GB300_OK;
+}
+
+// Slab entry records and actuation parameters from the host spring arrays.
+int upload_entries(titan_gb300_sim *s) {
+    const tg::Plan &P = s->plan;
+    const size_t E = P.ent_ends.size();
+    auto &a = s->args;
+    if (E == 0) return TITAN_GB300_OK;
+    auto sp_amp = [&](int64_t j) { return s->amp.empty() ? 0.2 : s->amp[j]; };
+    auto sp_phase = [&](int64_t j) { return s->phase.empty() ? 0.0 : s->phase[j]; };
+    auto sp_omega = [&](int64_t j) { return s->omega.empty() ? 0.0 : s->omega[j]; };
+    if (s->prec == P_FP64) {
+        std::vector<double> ent(4 * E), act(4 * E, 0.0);
+        for (size_t e = 0; e < E; e++) {
+            int64_t j = P.ent_spring[e];
+            ent[4 * e] = s->k[j];
+            ent[4 * e + 1] = s->rest[j];
+            ent[4 * e + 2] = s->damping[j];
+            uint64_t bits = P.ent_ends[e];
+            std::memcpy(&ent[4 * e + 3], &bits, 8);
+            act[4 * e] = sp_omega(j);
+            act[4 * e + 1] = sp_amp(j);
+            act[4 * e + 2] = sp_phase(j);
+        }
+        CK(cudaMemcpy(const_cast<void *>(a.ent), ent.data(), ent.size() * 8, cudaMemcpyHostToDevice), "upload ent");
+        CK(cudaMemcpy(const_cast<void *>(a.act), act.data(), act.size() * 8, cudaMemcpyHostToDevice), "upload act");
+    } else {
+        std::vector<float> ent(4 * E), act(4 * E, 0.f);
+        for (size_t e = 0; e < E; e++) {
+            int64_t j = P.ent_spring[e];
+            uint32_t bits = P.ent_ends[e];
+            std::memcpy(&ent[4 * e], &bits, 4);
+            ent[4 * e + 1] = (float)s->k[j];
+            ent[4 * e + 2] = (float)s->rest[j];
+            ent[4 * e + 3] = (float)s->damping[j];
+            act[4 * e] = (float)sp_omega(j);
+            act[4 * e + 1] = (float)sp_amp(j);
+            act[4 * e + 2] = (float)sp_phase(j);
+        }
+        CK(cudaMemcpy(const_cast<void *>(a.ent), ent.data(), ent.size() * 4, cudaMemcpyHostToDevice), "upload ent");
+        CK(cudaMemcpy(const_cast<void *>(a.act), act.data(), act.size() * 4, cudaMemcpyHostToDevice), "upload act");
+    }
+    return TITAN_GB300_OK;
+}
+
+template <typename T>
+T *dev_copy(titan_gb300_sim *s, const std::vector<T> &v, cudaError_t &e) {
+    T *p = (T *)s->mem.get(v.size() * sizeof(T), e);
+    if (!p) return nullptr;
+    if (!v.empty()) e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? p : nullptr;
+}
+
+tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
+    tg::PlanInput in;
+    in.n = s->n;
+    in.pos = s->pos.data();
+    in.fixed = s->fixed.empty() ? nullptr : s->fixed.data();
+    in.ns = s->ns;
+    in.left = s->left.data();
+    in.right = s->right.data();
+    in.type = s->type.empty() ? nullptr : s->type.data();
+    in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
+    in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 256 : 512);
+    in.heavy_threshold = 96;
+    // shared-memory budget: slab entries must fit beside the staged state
+    const size_t budget = 220 * 1024;
+    const size_t rs = s->rsize();
+    const int state_words = s->prec == P_FP32C ? 9 : 6;
+    in.slot_cap = std::min<int>(4095, std::max<int>(1024, in.tile_cap * 4));
+    long ecap = (long)((budget - (size_t)in.slot_cap * state_words * rs) / (3 * rs)) - 3 * 64;
+    in.entry_cap = (int)std::min<long>(32767, std::max<long>(ecap, 64));
+    return in;
+}
+
+// Builds the plan and all device buffers; positions/velocities come from the
+// host mirror.  Keeps T / steps.
+int build_device(titan_gb300_sim *s) {
+    s->free_device();
+    tg::PlanInput in = plan_input(s, s->tile_masses);
+    const size_t rs = s->rsize();
+    std::string why = tg::build_plan(in, s->plan);
+    if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    const tg::Plan &P = s->plan;
+    s->threads = std::max(32, std::min(512, ((P.max_nm + 31) / 32) * 32));
+    if (s->threads < 128) s->threads = 128;
+    s->npad = ((s->n + 127) / 128) * 128;
+    const int64_t np = s->npad;
+    auto &a = s->args;
+    a = tg::StepArgs{};
+    a.npad = np;
+    a.slots = std::max(P.max_slots, 1);
+    a.ecap = std::max(P.max_entries, 1);
+    a.hcap = std::max(P.max_heavy, 1);
+    s->smem = tg::step_smem_bytes(s->prec, a.slots, a.ecap, P.max_heavy > 0 ? a.hcap : 0);
+    if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
+    CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
+
+    cudaError_t e = cudaSuccess;
+    std::vector<tg::TileInfo> tiles(P.ntiles);
+    for (int64_t t = 0; t < P.ntiles; t++) {
+        tg::TileInfo &ti = tiles[t];
+        ti.mass_off = (int32_t)P.tile_mass_off[t];
+        ti.nm = (int32_t)(P.tile_mass_off[t + 1] - P.tile_mass_off[t]);
+        ti.halo_off = (int32_t)P.tile_halo_off[t];
+        ti.nh = (int32_t)(P.tile_halo_off[t + 1] - P.tile_halo_off[t]);
+        ti.ent_off = (int32_t)P.tile_ent_off[t];
+        ti.ne = (int32_t)(P.tile_ent_off[t + 1] - P.tile_ent_off[t]);
+        ti.nact = P.tile_nact[t];
+        ti.warp_off = (int32_t)P.tile_warp_off[t];
+        ti.heavy_off = (int32_t)P.tile_heavy_off[t];
+        ti.nheavy = (int32_t)(P.tile_heavy_off[t + 1] - P.tile_heavy_off[t]);
+        ti.body = P.body_of_tile[t];
+        ti.pad = 0;
+    }
+    if (P.ent_ends.size() > (size_t)INT32_MAX || P.halo.size() > (size_t)INT32_MAX)
+        return s->fail(TITAN_GB300_ELIMIT, "more than 2^31 slab entries");
+#define DEVCOPY(dst, vec, what)                               \
+    do {                                                      \
+        auto *p_ = dev_copy(s, vec, e);                       \
+        if (!p_) return s->cuda_fail(e, what);                \
+        dst = p_;                                             \
+    } while (0)
+    DEVCOPY(a.tiles, tiles, "upload tiles");
+    DEVCOPY(a.halo, P.halo, "upload halo");
+    DEVCOPY(a.warp_inc_off, P.warp_inc_off, "upload warp offsets");
+    std::vector<uint8_t> deg(np, 0);
+    std::copy(P.deg.begin(), P.deg.end(), deg.begin());
+    DEVCOPY(a.deg, deg, "upload degrees");
+    DEVCOPY(a.inc, P.inc, "upload incidence");
+    DEVCOPY(a.heavy_local, P.heavy_local, "upload heavy");
+    DEVCOPY(a.heavy_inc_off, P.heavy_inc_off, "upload heavy");
+    DEVCOPY(a.heavy_inc, P.heavy_inc, "upload heavy");
+    DEVCOPY(s->d_old2new, P.old2new, "upload order");
+    std::vector<double> bp(6 * std::max<size_t>(1, s->body_plane.size()), 0.0);
+    for (size_t b = 0; b < s->body_plane.size(); b++)
+        for (int c = 0; c < 6; c++) bp[6 * b + c] = s->body_plane[b][c];
+    std::vector<float> bpf(bp.begin(), bp.end());
+    DEVCOPY(a.body_plane, bp, "upload body planes");
+    DEVCOPY(a.body_planef, bpf, "upload body planes");
+#undef DEVCOPY
+    const size_t E = std::max<size_t>(1, P.ent_ends.size());
+    const size_t rs4 = (s->prec == P_FP64 ? 32 : 16);
+    if (!(a.ent = s->mem.get(E * rs4, e))) return s->cuda_fail(e, "alloc entries");
+    if (!(a.act = s->mem.get(E * rs4, e))) return s->cuda_fail(e, "alloc actuation");
+    if (!(a.mass = s->mem.get(np * rs, e))) return s->cuda_fail(e, "alloc mass");
+    if (!(a.flags = (const uint8_t *)s->mem.get(np, e))) return s->cuda_fail(e, "alloc flags");
+    if (!(a.ext = s->mem.get(3 * np * rs, e))) return s->cuda_fail(e, "alloc ext");
+    if (!(a.drag = (const int32_t *)s->mem.get(np * 4, e))) return s->cuda_fail(e, "alloc drag");
+    if (!(a.lc_ptr = (const int32_t *)s->mem.get((np + 1) * 4, e))) return s->cuda_fail(e, "alloc lc");
+    if (!(a.state0 = s->mem.get(s->comps() * np * rs, e))) return s->cuda_fail(e, "alloc state");
+    if (!(a.state1 = s->mem.get(s->comps() * np * rs, e))) return s->cuda_fail(e, "alloc state");
+    if (!(a.acc = s->mem.get(3 * np * rs, e))) return s->cuda_fail(e, "alloc acc");
+    if (!(a.tbuf = (double *)s->mem.get(2 * sizeof(double), e))) return s->cuda_fail(e, "alloc time");
+    if (!(s->dprm = (tg::DevParams *)s->mem.get(sizeof(tg::DevParams), e))) return s->cuda_fail(e, "alloc params");
+    a.prm = s->dprm;
+    if (!(s->d_xfer = (double *)s->mem.get(9 * (size_t)s->n * 8, e))) return s->cuda_fail(e, "alloc staging");
+    if (!(s->d_idx = (int64_t *)s->mem.get((size_t)s->n * 8, e))) return s->cuda_fail(e, "alloc staging");
+    CK(cudaMallocHost(&s->h_xfer, 9 * (size_t)s->n * 8), "alloc pinned staging");
+    CK(cudaMemset(a.state0, 0, s->comps() * np * rs), "clear state");
+    CK(cudaMemset(a.state1, 0, s->comps() * np * rs), "clear state");
+    CK(cudaMemset(a.acc, 0, 3 * np * rs), "clear acc");
+
+    int rc = upload_entries(s);
+    if (rc) return rc;
+    rc = upload_mass_attrs(s);
+    if (rc) return rc;
+    // positions / velocities into both ping-pong buffers
+    std::memcpy(s->h_xfer, s->pos.data(), 3 * s->n * 8);
+    std::memcpy(s->h_xfer + 3 * s->n, s->vel.data(), 3 * s->n * 8);
+    CK(cudaMemcpy(s->d_xfer, s->h_xfer, 6 * s->n * 8, cudaMemcpyHostToDevice), "upload state");
+    tg::XferArgs x{};
+    x.old2new = s->d_old2new;
+    x.count = s->n;
+    x.npad = np;
+    x.state0 = a.state0;
+    x.state1 = a.state1;
+    x.acc = a.acc;
+    x.ipos = s->d_xfer;
+    x.ivel = s->d_xfer + 3 * s->n;
+    CK(tg::launch_scatter(s->prec, x, s->stream), "scatter state");
+    s->parity = 0;
+    rc = upload_params(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "start");
+    return TITAN_GB300_OK;
+}
+
+// Downloads positions/velocities into the host mirror (creation order).
+int pull_state(titan_gb300_sim *s) {
+    tg::XferArgs x{};
+    x.old2new = s->d_old2new;
+    x.count = s->n;
+    x.npad = s->npad;
+    x.state0 = s->args.state0;
+    x.state1 = s->args.state1;
+    x.acc = s->args.acc;
+    x.parity = s->parity;
+    x.pos = s->d_xfer;
+    x.vel = s->d_xfer + 3 * s->n;
+    CK(tg::launch_gather(s->prec, x, s->stream), "gather state");
+    CK(cudaMemcpyAsync(s->h_xfer, s->d_xfer, 6 * s->n * 8, cudaMemcpyDeviceToHost, s->stream), "download");
+    CK(cudaStreamSynchronize(s->stream), "download");
+    std::memcpy(s->pos.data(), s->h_xfer, 3 * s->n * 8);
+    std::memcpy(s->vel.data(), s->h_xfer + 3 * s->n, 3 * s->n * 8);
+    return TITAN_GB300_OK;
+}
+
+// Per-mass local time: the reference adds dt to each free mass every step
+// (src/sim.cu:1165); replay those additions from the mass's last upload.
+void mass_times(titan_gb300_sim *s, const int64_t *idx, int64_t count, double *T) {
+    std::map<std::pair<uint64_t, int64_t>, double> memo;
+    for (int64_t q = 0; q < count; q++) {
+        int64_t i = idx ? idx[q] : q;
+        if (!s->fixed.empty() && s->fixed[i]) {
+            T[q] = s->mT0[i];
+            continue;
+        }
+        uint64_t bits;
+        std::memcpy(&bits, &s->mT0[i], 8);
+        auto key = std::make_pair(bits, s->mTstep[i]);
+        auto it = memo.find(key);
+        if (it != memo.end()) {
+            T[q] = it->second;
+            continue;
+        }
+        double t = s->mT0[i];
+        int64_t st = s->mTstep[i];
+        for (size_t r = 0; r < s->dt_log.size(); r++) {
+            int64_t b = s->dt_log[r].first;
+            int64_t e = r + 1 < s->dt_log.size() ? s->dt_log[r + 1].first : s->steps;
+            double d = s->dt_log[r].second;
+            for (int64_t z = std::max(b, st); z < e; z++) t = t + d;
+        }
+        memo[key] = t;
+        T[q] = t;
+    }
+}
+
+cudaGraphExec_t get_graph(titan_gb300_sim *s, int len, int parity, cudaError_t &e) {
+    auto key = std::make_pair(len, parity);
+    auto it = s->graphs.find(key);
+    if (it != s->graphs.end()) return it->second;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return nullptr;
+    int p = parity;
+    for (int i = 0; i < len; i++) {
+        tg::launch_step(s->prec, s->args, (int)s->plan.ntiles, s->threads, s->smem, p, 0, s->stream);
+        p ^= 1;
+    }
+    e = cudaStreamEndCapture(s->stream, &g);
+    if (e != cudaSuccess) return nullptr;
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return nullptr;
+    s->graphs[key] = ex;
+    return ex;
+}
+
+bool ensure_device(titan_gb300_sim *s) { return cudaSetDevice(s->device) == cudaSuccess; }
+
+}  // namespace
+
+extern "C" {
+
+const char *titan_gb300_version(void) { return "titan_gb300 0.1 (sm_103a)"; }
+
+int titan_gb300_create(titan_gb300_sim **out, int device, int precision) {
+    if (!out) return TITAN_GB300_EINVAL;
+    *out = nullptr;
+    if (precision < 0 || precision > 2 || device < 0) return TITAN_GB300_EINVAL;
+    // No CUDA call here: the device and stream are taken at start(), so a
+    // scene can be built and planned on a host without a GPU.
+    auto *s = new (std::nothrow) titan_gb300_sim();
+    if (!s) return TITAN_GB300_ENOMEM;
+    s->device = device;
+    s->prec = precision;
+    *out = s;
+    return TITAN_GB300_OK;
+}
+
+void titan_gb300_destroy(titan_gb300_sim *s) {
+    if (!s) return;
+    if (s->stream) ensure_device(s);
+    delete s;
+}
+
+int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "plan_host is for scenes that have not started");
+    if (s->n <= 0) return s->fail(TITAN_GB300_EINVAL, "no masses");
+    tg::PlanInput in = plan_input(s, tile_masses);
+    std::string why = tg::build_plan(in, s->plan);
+    if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    return TITAN_GB300_OK;
+}
+
+int64_t titan_gb300_plan_table(const titan_gb300_sim *s, int table, void *out) {
+    if (!s) return -1;
+    const tg::Plan &P = s->plan;
+    auto put = [&](const auto &v) -> int64_t {
+        if (out && !v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(v[0]));
+        return (int64_t)v.size();
+    };
+    switch (table) {
+        case TITAN_GB300_T_NEW2OLD: return put(P.new2old);
+        case TITAN_GB300_T_TILE_MASS_OFF: return put(P.tile_mass_off);
+        case TITAN_GB300_T_TILE_HALO_OFF: return put(P.tile_halo_off);
+        case TITAN_GB300_T_HALO: return put(P.halo);
+        case TITAN_GB300_T_TILE_ENT_OFF: return put(P.tile_ent_off);
+        case TITAN_GB300_T_TILE_NACT: return put(P.tile_nact);
+        case TITAN_GB300_T_ENT_ENDS: return put(P.ent_ends);
+        case TITAN_GB300_T_ENT_SPRING: return put(P.ent_spring);
+        case TITAN_GB300_T_TILE_WARP_OFF: return put(P.tile_warp_off);
+        case TITAN_GB300_T_WARP_INC_OFF: return put(P.warp_inc_off);
+        case TITAN_GB300_T_DEG: return put(P.deg);
+        case TITAN_GB300_T_INC: return put(P.inc);
+        case TITAN_GB300_T_TILE_HEAVY_OFF: return put(P.tile_heavy_off);
+        case TITAN_GB300_T_HEAVY_LOCAL: return put(P.heavy_local);
+        case TITAN_GB300_T_HEAVY_INC_OFF: return put(P.heavy_inc_off);
+        case TITAN_GB300_T_HEAVY_INC: return put(P.heavy_inc);
+        case TITAN_GB300_T_BODY_OF_TILE: return put(P.body_of_tile);
+        default: return -1;
+    }
+}
+
+const char *titan_gb300_last_error(const titan_gb300_sim *s) {
+    return s ? s->err.c_str() : "null handle";
+}
+
+int titan_gb300_set_masses(titan_gb300_sim *s, int64_t n, const double *pos, const double *vel,
+                           const double *m, const double *ext, const uint8_t *fixed, const double *drag) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "masses can only be replaced before start");
+    if (n <= 0 || !pos || !m) return s->fail(TITAN_GB300_EINVAL, "need n > 0, pos and m");
+    s->n = n;
+    s->pos.assign(pos, pos + 3 * n);
+    s->vel.assign(3 * n, 0.0);
+    if (vel) s->vel.assign(vel, vel + 3 * n);
+    s->m.assign(m, m + n);
+    s->ext.clear();
+    if (ext) s->ext.assign(ext, ext + 3 * n);
+    s->fixed.clear();
+    if (fixed) s->fixed.assign(fixed, fixed + n);
+    s->drag.clear();
+    if (drag) {
+        s->drag.resize(n);
+        for (int64_t i = 0; i < n; i++) s->drag[i] = (int32_t)drag[i];  // object.h:213 truncation
+    }
+    s->lc_ptr.clear();
+    s->lc_type.clear();
+    s->lc_rec.clear();
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_springs(titan_gb300_sim *s, int64_t n, const int32_t *left, const int32_t *right,
+                            const double *k, const double *rest, const double *damping,
+                            const int32_t *type, const double *omega, const double *amp,
+                            const double *phase) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "springs can only be replaced before start");
+    if (n < 0 || (n > 0 && (!left || !right || !k || !rest))) return s->fail(TITAN_GB300_EINVAL, "bad springs");
+    s->ns = n;
+    s->left.assign(left, left + n);
+    s->right.assign(right, right + n);
+    s->k.assign(k, k + n);
+    s->rest.assign(rest, rest + n);
+    s->damping.assign(n, 0.0);
+    if (damping) s->damping.assign(damping, damping + n);
+    s->type.clear();
+    if (type) {
+        s->type.assign(type, type + n);
+        for (int32_t t : s->type)
+            if (t < 0 || t > 3) return s->fail(TITAN_GB300_EINVAL, "spring type must be 0..3");
+    }
+    s->omega.clear();
+    if (omega) s->omega.assign(omega, omega + n);
+    s->amp.clear();
+    if (amp) s->amp.assign(amp, amp + n);
+    s->phase.clear();
+    if (phase) s->phase.assign(phase, phase + n);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_local_constraints(titan_gb300_sim *s, const int64_t *mass_ptr, const int32_t *type,
+                                      const double *vec, const double *num) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "set local constraints before start");
+    if (s->n <= 0 || !mass_ptr) return s->fail(TITAN_GB300_EINVAL, "set masses first");
+    int64_t nr = mass_ptr[s->n];
+    if (mass_ptr[0] != 0 || nr < 0) return s->fail(TITAN_GB300_EINVAL, "bad record offsets");
+    static const int order[4] = {1, 2, 0, 3};  // contact, ball, constraint plane, direction
+    s->lc_ptr.assign(s->n + 1, 0);
+    s->lc_type.clear();
+    s->lc_rec.clear();
+    for (int64_t i = 0; i < s->n; i++) {
+        if (mass_ptr[i + 1] < mass_ptr[i]) return s->fail(TITAN_GB300_EINVAL, "bad record offsets");
+        for (int o = 0; o < 4; o++)
+            for (int64_t r = mass_ptr[i]; r < mass_ptr[i + 1]; r++) {
+                if (type[r] != order[o]) continue;
+                double v[3] = {vec[3 * r], vec[3 * r + 1], vec[3 * r + 2]};
+                if (type[r] != TITAN_GB300_BALL) {  // constructors normalise (object.cu:60,109,127)
+                    double nn = norm3(v);
+                    if (nn == 0.0) return s->fail(TITAN_GB300_EINVAL, "zero constraint vector");
+                    for (double &c : v) c = c / nn;
+                }
+                s->lc_type.push_back(type[r]);
+                s->lc_rec.insert(s->lc_rec.end(), {v[0], v[1], v[2], num[r]});
+            }
+        s->lc_ptr[i + 1] = (int64_t)s->lc_type.size();
+    }
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double offset, double fk, double fs) {
+    if (!s || !normal) return TITAN_GB300_EINVAL;
+    if ((int)s->planes.size() >= tg::kMaxPlanes) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global planes");
+    double nn = norm3(normal);
+    if (!(nn > 0)) return s->fail(TITAN_GB300_EINVAL, "zero plane normal");
+    s->planes.push_back({normal[0] / nn, normal[1] / nn, normal[2] / nn, offset, fk, fs});
+    if (s->started) return upload_params(s);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_add_ball(titan_gb300_sim *s, const double center[3], double radius) {
+    if (!s || !center) return TITAN_GB300_EINVAL;
+    if ((int)s->balls.size() >= tg::kMaxBalls) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global balls");
+    s->balls.push_back({center[0], center[1], center[2], radius});
+    if (s->started) return upload_params(s);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_clear_constraints(titan_gb300_sim *s) {
+    if (!s) return TITAN_GB300_EINVAL;
+    s->planes.clear();
+    s->balls.clear();
+    if (s->started) return upload_params(s);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!(dt > 0)) return s->fail(TITAN_GB300_EINVAL, "Cannot set time step to negative or zero value.");
+    s->dt = dt;
+    if (s->started) {
+        s->dt_log.emplace_back(s->steps, dt);
+        return upload_params(s);
+    }
+    return TITAN_GB300_OK;
+}
+
+double titan_gb300_get_time_step(const titan_gb300_sim *s) { return s ? s->dt : 0.0; }
+
+int titan_gb300_set_global_acc(titan_gb300_sim *s, const double g[3]) {
+    if (!s || !g) return TITAN_GB300_EINVAL;
+    for (int c = 0; c < 3; c++) s->g[c] = g[c];
+    if (s->started) return upload_params(s);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_bodies(titan_gb300_sim *s, int64_t nbodies, const int64_t *mass_ptr) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "set bodies before start");
+    if (nbodies <= 0 || !mass_ptr || mass_ptr[0] != 0 || mass_ptr[nbodies] != s->n)
+        return s->fail(TITAN_GB300_EINVAL, "body ranges must cover all masses");
+    for (int64_t b = 0; b < nbodies; b++)
+        if (mass_ptr[b + 1] <= mass_ptr[b]) return s->fail(TITAN_GB300_EINVAL, "empty body");
+    s->body_ptr.assign(mass_ptr, mass_ptr + nbodies + 1);
+    s->body_plane.assign(nbodies, {0, 0, 1, 0, 0, 0});
+    s->body_has_plane.assign(nbodies, 0);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_body_plane(titan_gb300_sim *s, int64_t body, const double normal[3], double offset,
+                               double fk, double fs) {
+    if (!s || !normal) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "set body planes before start");
+    if (body < 0 || body >= (int64_t)s->body_plane.size()) return s->fail(TITAN_GB300_EINVAL, "no such body");
+    double nn = norm3(normal);
+    if (!(nn > 0)) return s->fail(TITAN_GB300_EINVAL, "zero plane normal");
+    s->body_plane[body] = {normal[0] / nn, normal[1] / nn, normal[2] / nn, offset, fk, fs};
+    s->body_has_plane[body] = 1;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_start(titan_gb300_sim *s, int tile_masses) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (s->n <= 0)
+        return s->fail(TITAN_GB300_EINVAL, "No masses have been added. Please add masses before starting the simulation.");
+    if (!(s->dt > 0)) return s->fail(TITAN_GB300_EINVAL, "invalid time step");
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    if (!s->stream) CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "create stream");
+    s->tile_masses = tile_masses;
+    s->T = 0.0;
+    s->steps = 0;
+    s->dt_log.assign(1, {0, s->dt});
+    s->mT0.assign(s->n, 0.0);
+    s->mTstep.assign(s->n, 0);
+    int rc = build_device(s);
+    if (rc) return rc;
+    s->started = true;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (nsteps < 0) return s->fail(TITAN_GB300_EINVAL, "negative step count");
+    if (nsteps == 0) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    cudaError_t e = cudaSuccess;
+    int64_t rem = nsteps - 1;
+    while (rem > 0) {
+        int len = (int)std::min<int64_t>(rem, kChunk);
+        cudaGraphExec_t g = get_graph(s, len, s->parity, e);
+        if (!g) return s->cuda_fail(e, "build step graph");
+        CK(cudaGraphLaunch(g, s->stream), "launch step graph");
+        s->parity ^= (len & 1);
+        rem -= len;
+    }
+    CK(tg::launch_step(s->prec, s->args, (int)s->plan.ntiles, s->threads, s->smem, s->parity, 1, s->stream),
+       "launch step");
+    s->parity ^= 1;
+    for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
+    s->steps += nsteps;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_synchronize(titan_gb300_sim *s) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->stream) return TITAN_GB300_OK;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return TITAN_GB300_OK;
+}
+
+double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }
+
+int titan_gb300_set_time(titan_gb300_sim *s, double T) {
+    if (!s) return TITAN_GB300_EINVAL;
+    s->T = T;
+    if (!s->started) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    return upload_params(s);
+}
+int64_t titan_gb300_steps(const titan_gb300_sim *s) { return s ? s->steps : 0; }
+
+int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx, double *pos, double *vel,
+                           double *acc, double *T) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (count < 0 || count > s->n) return s->fail(TITAN_GB300_EINVAL, "bad count");
+    if (idx)
+        for (int64_t q = 0; q < count; q++)
+            if (idx[q] < 0 || idx[q] >= s->n) return s->fail(TITAN_GB300_EINVAL, "mass index out of range");
+    if (count == 0) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    tg::XferArgs x{};
+    x.old2new = s->d_old2new;
+    x.count = count;
+    x.npad = s->npad;
+    x.state0 = s->args.state0;
+    x.state1 = s->args.state1;
+    x.acc = s->args.acc;
+    x.parity = s->parity;
+    if (idx) {
+        CK(cudaMemcpyAsync(s->d_idx, idx, count * 8, cudaMemcpyHostToDevice, s->stream), "upload index");
+        x.idx = s->d_idx;
+    }
+    x.pos = pos ? s->d_xfer : nullptr;
+    x.vel = vel ? s->d_xfer + 3 * count : nullptr;
+    x.accout = acc ? s->d_xfer + 6 * count : nullptr;
+    if (pos || vel || acc) {
+        CK(tg::launch_gather(s->prec, x, s->stream), "gather");
+        CK(cudaMemcpyAsync(s->h_xfer, s->d_xfer, 9 * count * 8, cudaMemcpyDeviceToHost, s->stream), "download");
+    }
+    CK(cudaStreamSynchronize(s->stream), "download");
+    if (pos) std::memcpy(pos, s->h_xfer, 3 * count * 8);
+    if (vel) std::memcpy(vel, s->h_xfer + 3 * count, 3 * count * 8);
+    if (acc) std::memcpy(acc, s->h_xfer + 6 * count, 3 * count * 8);
+    if (T) mass_times(s, idx, count, T);
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_get_state(titan_gb300_sim *s, double *pos, double *vel, double *acc, double *T) {
+    if (!s) return TITAN_GB300_EINVAL;
+    return titan_gb300_get_masses(s, s->n, nullptr, pos, vel, acc, T);
+}
+
+int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t *idx, const double *pos,
+                               const double *vel, const double *m, const double *ext, const uint8_t *fixed,
+                               const double *drag, const double *T) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (!idx) count = s->n;
+    if (count < 0 || count > s->n) return s->fail(TITAN_GB300_EINVAL, "bad count");
+    for (int64_t q = 0; idx && q < count; q++)
+        if (idx[q] < 0 || idx[q] >= s->n) return s->fail(TITAN_GB300_EINVAL, "mass index out of range");
+    if (m)
+        for (int64_t q = 0; q < count; q++)
+            if (!(m[q] > 0)) return s->fail(TITAN_GB300_EINVAL, "mass must be positive");
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    CK(cudaStreamSynchronize(s->stream), "set");
+    bool replan = false;
+    if (fixed) {
+        if (s->fixed.empty()) s->fixed.assign(s->n, 0);
+        for (int64_t q = 0; q < count; q++) {
+            int64_t i = idx ? idx[q] : q;
+            if ((s->fixed[i] != 0) != (fixed[q] != 0)) replan = true;
+        }
+    }
+    // local time bookkeeping: masses whose T is given, or whose fixed flag
+    // flips, restart their clock here
+    std::vector<double> Tcur;
+    if (replan || T) {
+        Tcur.resize(s->n);
+        mass_times(s, nullptr, s->n, Tcur.data());
+    }
+    for (int64_t q = 0; q < count; q++) {
+        int64_t i = idx ? idx[q] : q;
+        if (m) s->m[i] = m[q];
+        if (ext) {
+            if (s->ext.empty()) s->ext.assign(3 * s->n, 0.0);
+            for (int c = 0; c < 3; c++) s->ext[3 * i + c] = ext[3 * q + c];
+        }
+        if (drag) {
+            if (s->drag.empty()) s->drag.assign(s->n, 0);
+            s->drag[i] = (int32_t)drag[q];
+        }
+        if (T || (fixed && (s->fixed[i] != 0) != (fixed[q] != 0))) {
+            s->mT0[i] = T ? T[q] : Tcur[i];
+            s->mTstep[i] = s->steps;
+        }
+        if (fixed) s->fixed[i] = fixed[q] ? 1 : 0;
+    }
+    if (replan) {
+        int rc = pull_state(s);
+        if (rc) return rc;
+        for (int64_t q = 0; q < count; q++) {
+            int64_t i = idx ? idx[q] : q;
+            for (int c = 0; c < 3; c++) {
+                if (pos) s->pos[3 * i + c] = pos[3 * q + c];
+                if (vel) s->vel[3 * i + c] = vel[3 * q + c];
+            }
+        }
+        s->drop_graphs();
+        return build_device(s);
+    }
+    if (m || ext || drag) {
+        int rc = upload_mass_attrs(s);
+        if (rc) return rc;
+    }
+    if (pos || vel) {
+        tg::XferArgs x{};
+        x.old2new = s->d_old2new;
+        x.count = count;
+        x.npad = s->npad;
+        x.state0 = s->args.state0;
+        x.state1 = s->args.state1;
+        x.acc = s->args.acc;
+        if (idx) {
+            CK(cudaMemcpyAsync(s->d_idx, idx, count * 8, cudaMemcpyHostToDevice, s->stream), "upload index");
+            x.idx = s->d_idx;
+        }
+        if (pos) std::memcpy(s->h_xfer, pos, 3 * count * 8);
+        if (vel) std::memcpy(s->h_xfer + 3 * count, vel, 3 * count * 8);
+        CK(cudaMemcpyAsync(s->d_xfer, s->h_xfer, 6 * count * 8, cudaMemcpyHostToDevice, s->stream), "upload");
+        x.ipos = pos ? s->d_xfer : nullptr;
+        x.ivel = vel ? s->d_xfer + 3 * count : nullptr;
+        CK(tg::launch_scatter(s->prec, x, s->stream), "scatter");
+        CK(cudaStreamSynchronize(s->stream), "set");
+    }
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64_t *idx, const double *k,
+                                  const double *rest, const double *damping, const int32_t *type,
+                                  const double *omega, const double *amp, const double *phase) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!idx) count = s->ns;
+    if (count < 0 || count > s->ns) return s->fail(TITAN_GB300_EINVAL, "bad count");
+    bool replan = false;
+    for (int64_t q = 0; q < count; q++) {
+        int64_t j = idx ? idx[q] : q;
+        if (j < 0 || j >= s->ns) return s->fail(TITAN_GB300_EINVAL, "spring index out of range");
+        if (type && (type[q] < 0 || type[q] > 3)) return s->fail(TITAN_GB300_EINVAL, "spring type must be 0..3");
+    }
+    for (int64_t q = 0; q < count; q++) {
+        int64_t j = idx ? idx[q] : q;
+        if (k) s->k[j] = k[q];
+        if (rest) s->rest[j] = rest[q];
+        if (damping) s->damping[j] = damping[q];
+        if (type) {
+            if (s->type.empty()) s->type.assign(s->ns, 0);
+            bool was = s->type[j] >= 2, now = type[q] >= 2;
+            if (was != now) replan = true;
+            s->type[j] = type[q];
+        }
+        if (omega) {
+            if (s->omega.empty()) s->omega.assign(s->ns, 0.0);
+            s->omega[j] = omega[q];
+        }
+        if (amp) {
+            if (s->amp.empty()) s->amp.assign(s->ns, 0.2);
+            s->amp[j] = amp[q];
+        }
+        if (phase) {
+            if (s->phase.empty()) s->phase.assign(s->ns, 0.0);
+            s->phase[j] = phase[q];
+        }
+    }
+    if (!s->started) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    CK(cudaStreamSynchronize(s->stream), "set springs");
+    if (replan) {
+        int rc = pull_state(s);
+        if (rc) return rc;
+        s->drop_graphs();
+        return build_device(s);
+    }
+    // type changes within passive or within active keep the slab order, but
+    // the type bits live in the entry words
+    if (type) {
+        for (size_t e = 0; e < s->plan.ent_ends.size(); e++) {
+            int64_t j = s->plan.ent_spring[e];
+            s->plan.ent_ends[e] = (s->plan.ent_ends[e] & 0x00ffffffu) | ((uint32_t)(s->type[j] & 3) << 24);
+        }
+    }
+    return upload_entries(s);
+}
+
+int titan_gb300_diagnostics(titan_gb300_sim *s, double g_mag, double energy[4], double momentum[6]) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    cudaError_t e = cudaSuccess;
+    if (!s->d_sl) {
+        std::vector<int32_t> sl(s->ns, -1), sr(s->ns, -1);
+        for (int64_t j = 0; j < s->ns; j++) {
+            int32_t l = s->left[j], r = s->right[j];
+            if (l < 0 || r < 0 || l >= s->n || r >= s->n) continue;
+            sl[j] = s->plan.old2new[l];
+            sr[j] = s->plan.old2new[r];
+        }
+        if (!(s->d_sl = dev_copy(s, sl, e))) return s->cuda_fail(e, "diag alloc");
+        if (!(s->d_sr = dev_copy(s, sr, e))) return s->cuda_fail(e, "diag alloc");
+        if (!(s->d_partials = (double *)s->mem.get(tg::kDiagBlocks * tg::kDiagQ * 8, e)))
+            return s->cuda_fail(e, "diag alloc");
+        if (!(s->d_dout = (double *)s->mem.get(tg::kDiagQ * 8, e))) return s->cuda_fail(e, "diag alloc");
+        if (!(s->d_sk = (double *)s->mem.get(std::max<int64_t>(1, s->ns) * 8, e))) return s->cuda_fail(e, "diag alloc");
+        if (!(s->d_srest = (double *)s->mem.get(std::max<int64_t>(1, s->ns) * 8, e)))
+            return s->cuda_fail(e, "diag alloc");
+    }
+    if (s->ns > 0) {
+        CK(cudaMemcpyAsync(s->d_sk, s->k.data(), s->ns * 8, cudaMemcpyHostToDevice, s->stream), "diag upload");
+        CK(cudaMemcpyAsync(s->d_srest, s->rest.data(), s->ns * 8, cudaMemcpyHostToDevice, s->stream), "diag upload");
+    }
+    tg::DiagArgs d{};
+    d.state = s->parity ? s->args.state1 : s->args.state0;
+    d.mass = s->args.mass;
+    d.n = s->n;
+    d.npad = s->npad;
+    d.sl = s->d_sl;
+    d.sr = s->d_sr;
+    d.sk = s->d_sk;
+    d.srest = s->d_srest;
+    d.ns = s->ns;
+    d.g_mag = g_mag;
+    d.partials = s->d_partials;
+    d.out = s->d_dout;
+    CK(tg::launch_diag(s->prec, d, s->stream), "diagnostics");
+    double out[tg::kDiagQ];
+    CK(cudaMemcpyAsync(out, s->d_dout, sizeof(out), cudaMemcpyDeviceToHost, s->stream), "diag download");
+    CK(cudaStreamSynchronize(s->stream), "diagnostics");
+    if (energy) {
+        energy[0] = out[0];
+        energy[1] = out[1];
+        energy[2] = out[2];
+        energy[3] = (out[0] + out[1]) + out[2];
+    }
+    if (momentum)
+        for (int c = 0; c < 6; c++) momentum[c] = out[3 + c];
+    return TITAN_GB300_OK;
+}
+
+void *titan_gb300_stream(titan_gb300_sim *s) { return s ? (void *)s->stream : nullptr; }
+
+int titan_gb300_plan_info(const titan_gb300_sim *s, int64_t out[12]) {
+    if (!s || !out) return TITAN_GB300_EINVAL;
+    const tg::Plan &P = s->plan;
+    std::memset(out, 0, 12 * sizeof(int64_t));
+    out[0] = s->n;
+    out[1] = s->ns;
+    if (!s->started) return TITAN_GB300_OK;
+    out[2] = P.ntiles;
+    out[3] = (int64_t)P.ent_ends.size();
+    out[4] = (int64_t)P.halo.size();
+    out[5] = (int64_t)P.inc.size();
+    out[6] = (int64_t)P.heavy_local.size();
+    out[7] = (int64_t)s->smem;
+    out[8] = s->threads;
+    int64_t nact_springs = 0;
+    if (!s->type.empty())
+        for (int32_t t : s->type) nact_springs += t >= 2;
+    int64_t nact_ent = 0;
+    for (int32_t a : P.tile_nact) nact_ent += a;
+    const bool f64 = s->prec == P_FP64;
+    // algorithmic bytes per step: per mass read x,v,m,flags + write x,v;
+    // per spring k, rest, damping + two endpoint indices; actuated springs
+    // add omega and phase.
+    int64_t mass_b = f64 ? 105 : (s->prec == P_FP32C ? 101 : 53);
+    int64_t spring_b = f64 ? 32 : 20, act_b = f64 ? 16 : 8;
+    out[9] = s->n * mass_b + P.valid_springs * spring_b + nact_springs * act_b;
+    // implementation bytes as laid out: per mass state read (+halo re-reads)
+    // and write, m, flags, degree; per entry record, act record, 2 B per
+    // incidence word, 4 B per halo index, tile table.
+    const int64_t rs = (int64_t)s->rsize();
+    const int64_t comps = s->comps();
+    int64_t impl = s->n * (comps * rs * 2 + rs + 1 + 1);
+    impl += (int64_t)P.ent_ends.size() * (f64 ? 32 : 16) + nact_ent * (f64 ? 32 : 16);
+    impl += (int64_t)P.inc.size() * 2 + (int64_t)P.heavy_inc.size() * 2 + (int64_t)P.halo.size() * 4;
+    impl += P.ntiles * (int64_t)sizeof(tg::TileInfo);
+    out[10] = impl;
+    out[11] = nact_ent;
+    return TITAN_GB300_OK;
+}
+
+int64_t titan_gb300_lattice_springs(int nx, int ny, int nz);
+
+}  // extern "C"

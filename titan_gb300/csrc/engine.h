@@ -1,0 +1,113 @@
+// engine.h -- device-side layout shared by the step kernels and the C ABI.
+//
+// HBM layout (all arrays in the tiled mass order of plan.h):
+//   state[2]   ping-pong buffers, component-major with stride npad:
+//              FP64  : x0 x1 x2 v0 v1 v2                      (double)
+//              FP32  : x0 x1 x2 v0 v1 v2                      (float)
+//              FP32C : xh0..2 vh0..2 xl0..2 vl0..2            (float hi/lo pairs)
+//   mass, flags  per-mass m and MF_* bits; ext/lc/drag are only read for
+//              masses whose flag asks for them.
+//   tiles      one TileInfo per CTA.
+//   ent        slab entries: FP64 {k, rest, damping, ends} (32 B),
+//              FP32 {ends, k, rest, damping} (16 B); act: {omega, amp, phase}.
+//   inc        per-warp ELL incidence (u16 entry index, 0x8000 = left end).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace tg {
+
+enum { P_FP64 = 0, P_FP32 = 1, P_FP32C = 2 };
+enum { MF_FIXED = 1, MF_EXT = 2, MF_LOCAL = 4, MF_DRAG = 8, MF_BODYPLANE = 16 };
+
+constexpr int kMaxPlanes = 16;
+constexpr int kMaxBalls = 16;
+
+struct TileInfo {
+    int32_t mass_off, nm, halo_off, nh;
+    int32_t ent_off, ne, nact, warp_off;
+    int32_t heavy_off, nheavy, body, pad;
+};
+
+struct DevParams {
+    double dt;
+    double g[3];
+    int32_t nplanes, nballs;
+    double plane[kMaxPlanes][6];  // normal xyz, offset, friction_k, friction_s
+    double ball[kMaxBalls][4];    // center xyz, radius
+    float dt_hi, dt_lo;
+    float gf[3];
+    float pad;
+    float planef[kMaxPlanes][6];
+    float ballf[kMaxBalls][4];
+};
+
+struct StepArgs {
+    const TileInfo *tiles;
+    const int32_t *halo;
+    const void *ent;
+    const void *act;
+    const uint32_t *warp_inc_off;
+    const uint8_t *deg;
+    const uint16_t *inc;
+    const uint16_t *heavy_local;
+    const uint32_t *heavy_inc_off;
+    const uint16_t *heavy_inc;
+    const void *mass;
+    const uint8_t *flags;
+    const void *ext;           // 3 * npad, component-major
+    const int32_t *lc_ptr;     // npad + 1
+    const int32_t *lc_type;
+    const double *lc_rec;      // 4 per record: vec xyz, num
+    const int32_t *drag;
+    const double *body_plane;  // 6 per body
+    const float *body_planef;  // same, single precision
+    void *state0;
+    void *state1;
+    void *acc;                 // 3 * npad
+    double *tbuf;              // [2]: T of the step with parity p is tbuf[p]
+    const DevParams *prm;
+    int64_t npad;
+    int32_t slots, ecap, hcap;
+};
+
+// Per-mass gather / scatter between caller order and tiled order.
+struct XferArgs {
+    const int32_t *old2new;
+    const int64_t *idx;        // caller indices, or null for 0..count-1
+    int64_t count;
+    int64_t npad;
+    void *state0;
+    void *state1;
+    void *acc;
+    int parity;
+    double *pos, *vel, *accout;  // gather outputs (3*count), any may be null
+    const double *ipos, *ivel;   // scatter inputs (3*count), any may be null
+};
+
+struct DiagArgs {
+    const void *state;
+    const void *mass;
+    int64_t n, npad;
+    const int32_t *sl, *sr;     // springs (new numbering), -1 = skipped
+    const double *sk, *srest;
+    int64_t ns;
+    double g_mag;
+    double *partials;           // kDiagBlocks * kDiagQ
+    double *out;                // kDiagQ
+};
+constexpr int kDiagBlocks = 512;
+constexpr int kDiagQ = 9;
+
+size_t step_smem_bytes(int precision, int slots, int ecap, int hcap);
+cudaError_t step_prepare(int precision, size_t smem);
+cudaError_t launch_step(int precision, const StepArgs &a, int ntiles, int threads, size_t smem,
+                        int parity, int write_acc, cudaStream_t s);
+cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
+cudaError_t launch_scatter(int precision, const XferArgs &a, cudaStream_t s);
+cudaError_t launch_diag(int precision, const DiagArgs &a, cudaStream_t s);
+
+}  // namespace tg

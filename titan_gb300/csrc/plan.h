@@ -1,0 +1,67 @@
+// plan.h -- host-side tile plan for the fused step kernel.
+//
+// The reference launches one thread per spring that atomically adds its force
+// into both endpoint masses (src/sim.cu:1046-1080, src/vec.cu:33-37), then one
+// thread per mass (src/sim.cu:1093-1169).  Here masses are renumbered into
+// spatially compact tiles; each tile owns a slab of spring entries (every
+// spring touching the tile, stored once per tile it touches), a halo of
+// remote masses those entries read, and per-mass incidence lists into the slab
+// in ascending spring order.  One CTA per tile computes each slab entry once
+// and gathers per mass in a fixed order: deterministic, no float atomics.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tg {
+
+struct PlanInput {
+    int64_t n = 0;                       // masses
+    const double *pos = nullptr;         // 3n, used for the spatial order
+    const uint8_t *fixed = nullptr;      // n or null; fixed masses gather nothing
+    int64_t ns = 0;                      // springs
+    const int32_t *left = nullptr, *right = nullptr;
+    const int32_t *type = nullptr;       // ns or null; types 2,3 are actuated
+    int64_t nbodies = 0;                 // 0: one body
+    const int64_t *body_ptr = nullptr;   // nbodies+1, creation-order ranges
+    int tile_cap = 512;                  // masses per tile
+    int slot_cap = 4095;                 // tile + halo slots per tile (12-bit)
+    int entry_cap = 32767;               // slab entries per tile (15-bit)
+    int heavy_threshold = 96;            // degree above this: warp-cooperative
+};
+
+// Entry word: left slot | right slot << 12 | type << 24 (slots are tile-local:
+// [0, nm) tile masses, [nm, nm+nh) halo masses).
+inline uint32_t pack_ends(uint32_t a, uint32_t b, uint32_t type) {
+    return a | (b << 12) | ((type & 3u) << 24);
+}
+
+struct Plan {
+    int64_t n = 0, ns = 0, ntiles = 0, nbodies = 1;
+    std::vector<int32_t> new2old, old2new;   // mass renumbering
+    std::vector<int32_t> body_of_tile;
+    std::vector<int64_t> tile_mass_off;      // ntiles+1 (new mass index)
+    std::vector<int64_t> tile_halo_off;      // ntiles+1
+    std::vector<int32_t> halo;               // new mass indices
+    std::vector<int64_t> tile_ent_off;       // ntiles+1
+    std::vector<int32_t> tile_nact;          // actuated entries lead each slab
+    std::vector<uint32_t> ent_ends;
+    std::vector<int64_t> ent_spring;         // original spring index of each entry
+    std::vector<int64_t> tile_warp_off;      // ntiles+1 (global warp index)
+    std::vector<uint32_t> warp_inc_off;      // per warp, into inc (u16 words)
+    std::vector<uint8_t> deg;                // per new mass; 255 = heavy
+    std::vector<uint16_t> inc;               // entry | 0x8000 when the mass is the left end
+    std::vector<int64_t> tile_heavy_off;     // ntiles+1 (global heavy index)
+    std::vector<uint16_t> heavy_local;       // tile-local index of each heavy mass
+    std::vector<uint32_t> heavy_inc_off;     // nheavy+1, into heavy_inc
+    std::vector<uint16_t> heavy_inc;
+    int64_t valid_springs = 0;
+    int max_nm = 0, max_slots = 0, max_entries = 0, max_heavy = 0;
+};
+
+// Returns "" on success, otherwise the reason (e.g. a mass whose degree does
+// not fit one tile's slab).
+std::string build_plan(const PlanInput &in, Plan &out);
+
+}  // namespace tg
