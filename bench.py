@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--threads", type=int, default=0)
     return p.parse_args()
 
 
@@ -184,7 +185,7 @@ def run_ours(a, rank, world, local):
         barrier()
         return e0.elapsed_time(e1)
 
-    sim = wl.make_sim(sc, prec, a.tile, device=local)
+    sim = wl.make_sim(sc, prec, a.tile, device=local, threads=a.threads)
     info = sim.plan_info()
     sim.step(a.warmup)
     sim.synchronize()

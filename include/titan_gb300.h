@@ -138,6 +138,11 @@ int titan_gb300_set_body_plane(titan_gb300_sim *sim, int64_t body, const double 
  * the tuned default. */
 int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
 
+/* Launch shape of the step kernel: threads per CTA, a multiple of 32 in
+ * [64, 512], or 0 to derive it from the tile size.  Set before start(); the
+ * tile size itself is start()'s argument.  Used by the autotuner. */
+int titan_gb300_set_launch(titan_gb300_sim *sim, int threads_per_cta);
+
 /* One iteration of the reference's execute() loop body (src/sim.cu:1569-1590)
  * nsteps times: spring forces + mass update fused into one kernel per step,
  * replayed from cached CUDA graphs.  Asynchronous. */

@@ -1,0 +1,273 @@
+// The reference's physics tests (test/physics/*.cpp, googletest) re-expressed
+// without gtest against the drop-in header <Titan/sim.h>: same scenes, same
+// control calls, same tolerances.  Run one test per process:
+//     reference_physics <test_name>
+// Exit status 0 = pass.
+#include <Titan/sim.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <iostream>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+using titan::Vec;
+
+static int failures = 0;
+
+#define EXPECT_NEAR(a, b, tol)                                                                       \
+    do {                                                                                             \
+        double a_ = (a), b_ = (b), t_ = (tol);                                                       \
+        if (!(std::fabs(a_ - b_) <= t_)) {                                                           \
+            std::fprintf(stderr, "%s:%d: |%.9g - %.9g| > %.3g\n", __FILE__, __LINE__, a_, b_, t_);   \
+            failures++;                                                                              \
+        }                                                                                            \
+    } while (0)
+#define EXPECT_TRUE(c)                                                                 \
+    do {                                                                               \
+        if (!(c)) {                                                                    \
+            std::fprintf(stderr, "%s:%d: expected %s\n", __FILE__, __LINE__, #c);      \
+            failures++;                                                                \
+        }                                                                              \
+    } while (0)
+
+// test/testutil/utils.h:12-30 (gravity PE with the hard-coded 9.8).  The
+// penalty energy of masses below the z = 0 plane (20000 disp^2 / 2) is added:
+// the reference's util omits it, which makes a sample taken inside a contact
+// under-read by up to the whole kinetic energy.
+static double energy(titan::Simulation &sim) {
+    double pg = 0, ps = 0, ke = 0, pc = 0;
+    sim.getAll();
+    for (titan::Mass *m : sim.masses) {
+        pg += 9.8 * (m->pos)[2] * (m->m);
+        ke += 0.5 * (m->m) * std::pow((m->vel).norm(), 2);
+        if (m->pos[2] < 0) pc += 0.5 * 20000.0 * m->pos[2] * m->pos[2];
+    }
+    for (titan::Spring *s : sim.springs) ps += s->_k * std::pow((s->_left->pos - s->_right->pos).norm() - s->_rest, 2) / 2;
+    return ps + ke + pg + pc;
+}
+
+// test/physics/simple_unittest.cpp:15-34
+static void simple_test() {
+    titan::Simulation sim;
+    sim.createMass(Vec(1, 0, 1));
+    sim.setTimeStep(0.0001);
+    sim.setGlobalAcceleration(Vec(0, 0, -9.8));
+    sim.createPlane(Vec(0, 0, 1), 0);
+    sim.start();
+    double total = energy(sim), avg = total, alpha = 0.9;
+    while (sim.time() < 5) {
+        sim.wait(0.1);
+        avg = (1 - alpha) * energy(sim) + alpha * avg;
+        EXPECT_NEAR(avg, total, total * 0.01);
+        sim.resume();
+    }
+    sim.stop();
+}
+
+// test/physics/energy_unittest.cpp:14-40
+static void energy_test() {
+    titan::Simulation sim;
+    sim.createLattice(Vec(0, 0, 5), Vec(4, 4, 4), 20, 20, 20);
+    sim.setAllSpringConstantValues(1000);
+    sim.setTimeStep(0.0001);
+    sim.setGlobalAcceleration(Vec(0, 0, -9.8));
+    sim.defaultRestLengths();
+    sim.createPlane(Vec(0, 0, 1), 0);
+    sim.start();
+    double total = energy(sim), avg = total, alpha = 0.7;
+    while (sim.time() < 5) {
+        sim.wait(0.1);
+        avg = (1 - alpha) * energy(sim) + alpha * avg;
+        EXPECT_NEAR(avg, total, total * 0.01);
+        sim.resume();
+    }
+    sim.stop();
+}
+
+// test/physics/external_unittest.cpp:17-35
+static void external_test() {
+    titan::Simulation sim;
+    titan::Mass *m1 = sim.createMass(Vec(1, 0, 1));
+    sim.setTimeStep(0.0001);
+    m1->setExternalForce(m1->m * Vec(0, 0, -9.8));
+    sim.setGlobalAcceleration(Vec(0, 0, 0.0));
+    sim.start();
+    while (sim.time() < 5) {
+        sim.wait(0.1);
+        sim.getAll();
+        EXPECT_NEAR(m1->pos[0], 1, 1e-6);
+        EXPECT_NEAR(m1->pos[1], 0, 1e-6);
+        EXPECT_NEAR(m1->pos[2], 1 + 0.5 * -9.8 * std::pow(sim.time(), 2), 0.1);
+        sim.resume();
+    }
+    sim.stop();
+}
+
+// test/physics/external_unittest.cpp:38-56
+static void external_acc_test() {
+    titan::Simulation sim;
+    titan::Mass *m1 = sim.createMass(Vec(1, 0, 1));
+    sim.setTimeStep(0.0001);
+    m1->setExternalForce(m1->m * Vec(0, 0, 0));
+    sim.setGlobalAcceleration(Vec(0, 0, -9.8));
+    sim.start();
+    while (sim.time() < 1) {
+        sim.wait(0.1);
+        sim.getAll();
+        EXPECT_NEAR(m1->pos[0], 1, 1e-6);
+        EXPECT_NEAR(m1->pos[1], 0, 1e-6);
+        EXPECT_NEAR(m1->pos[2], 1 + 0.5 * -9.8 * std::pow(sim.time(), 2), 0.1);
+        sim.resume();
+    }
+    sim.stop();
+}
+
+// test/physics/multiagent_unittest.cpp:21-71 (smoke in the reference; here
+// also: time reached, positions finite)
+static void multiagent_test() {
+    const double SIZE = 5.0, SPACE = 3.0;
+    const int NUM_X = 10, NUM_Y = 10, DENSITY = 5;
+    titan::Simulation sim;
+    sim.setGlobalAcceleration(Vec(0, 0, -9.8));
+    titan::Lattice *grid[NUM_Y][NUM_X];
+    for (int i = 0; i < NUM_Y; i++)
+        for (int j = 0; j < NUM_X; j++)
+            grid[i][j] = sim.createLattice(Vec((SIZE + SPACE) * j + SIZE / 2, (SIZE + SPACE) * i + SIZE / 2, SIZE / 2),
+                                           Vec(SIZE, SIZE, SIZE), DENSITY, DENSITY, DENSITY);
+    std::vector<std::tuple<int, int>> right = {{100, 0}, {120, 20}, {104, 4}, {124, 24}};
+    std::vector<std::tuple<int, int>> up = {{20, 0}, {120, 100}, {124, 104}, {24, 4}};
+    for (int i = 0; i < NUM_Y - 1; i++)
+        for (int j = 0; j < NUM_X - 1; j++) {
+            for (auto pr : right) {
+                titan::Spring *s = sim.createSpring(grid[i][j]->masses[std::get<0>(pr)], grid[i][j + 1]->masses[std::get<1>(pr)]);
+                s->_k = 0.01;
+                s->defaultLength();
+            }
+            for (auto pr : up) {
+                titan::Spring *s = sim.createSpring(grid[i][j]->masses[std::get<0>(pr)], grid[i + 1][j]->masses[std::get<1>(pr)]);
+                s->_k = 0.01;
+                s->defaultLength();
+            }
+        }
+    sim.defaultRestLengths();
+    sim.start();
+    sim.pause(1.0);
+    sim.getAll();
+    EXPECT_TRUE(sim.time() >= 1.0 && sim.time() < 1.0 + 2 * sim.getTimeStep());
+    for (titan::Mass *m : sim.masses) EXPECT_TRUE(std::isfinite(m->pos[2]));
+    sim.stop();
+}
+
+// test/physics/rotate_unittest.cpp:11-40 (smoke in the reference)
+static void rotate_test() {
+    titan::Simulation sim;
+    titan::Lattice *l2 = sim.createLattice(Vec(0, 0, 10), Vec(5, 5, 5), 10, 10, 10);
+    sim.setAllSpringConstantValues(1E5);
+    l2->rotate(Vec(0, 0, 1), -0.78);
+    sim.createPlane(Vec(0, 0, 1), 0, 10, 10);
+    sim.setGlobalAcceleration(Vec(0, 0, -9.8));
+    sim.start();
+    while (true) {
+        sim.pause(sim.time() + 1);
+        sim.get(l2);
+        l2->rotate(Vec(0, 0, 1), 0.5);
+        sim.set(l2);
+        if (sim.time() > 5.0) {
+            for (titan::Mass *m : l2->masses) EXPECT_TRUE(std::isfinite(m->pos[2]));
+            sim.stop();
+            return;
+        }
+        sim.resume();
+    }
+}
+
+// ---- extensions ----
+
+// pause(t) stops at the first step whose accumulated time reaches t
+// (src/sim.cu:1505); step(n) then advances exactly n steps.
+static void breakpoint_and_step_test() {
+    titan::Simulation sim;
+    titan::Mass *m = sim.createMass(Vec(0, 0, 1));
+    sim.setTimeStep(0.0001);
+    sim.start();
+    sim.pause(0.05);
+    double t = 0;
+    long n = 0;
+    while (t < 0.05) {
+        t += 0.0001;
+        n++;
+    }
+    EXPECT_TRUE(sim.steps() == n);
+    EXPECT_TRUE(sim.time() == t);
+    sim.step(250);
+    EXPECT_TRUE(sim.steps() == n + 250);
+    sim.get(m);
+    double v = 0, z = 1;
+    for (long i = 0; i < n + 250; i++) {
+        v = v + ((-9.81 * 0.1) / 0.1) * 0.0001;
+        z = z + v * 0.0001;
+    }
+    EXPECT_NEAR(m->pos[2], z, 0.0);
+    EXPECT_NEAR(m->T, sim.time(), 1e-15);
+    sim.stop();
+}
+
+// Beam: the i == 0 face is fixed (src/object.cu:307-309) and never moves.
+static void beam_fixed_face_test() {
+    titan::Simulation sim;
+    titan::Beam *b = sim.createBeam(Vec(0, 0, 2), Vec(2, 0.5, 0.5), 8, 3, 3);
+    sim.start();
+    sim.pause(0.2);
+    sim.getAll();
+    for (int i = 0; i < 9; i++) EXPECT_NEAR(b->masses[i]->pos[2], 2 + (i % 3) * 0.25 - 0.25, 1e-15);
+    EXPECT_TRUE(b->masses.back()->pos[2] < 2.25);  // the free end sags
+    sim.stop();
+}
+
+// createMass / createSpring while paused (src/sim.cu:223-341): existing
+// masses keep their device state, new ones enter with their host state.
+static void topology_edit_test() {
+    titan::Simulation sim;
+    titan::Mass *a = sim.createMass(Vec(0, 0, 5));
+    sim.setGlobalAcceleration(Vec(0, 0, 0));
+    a->vel = Vec(1, 0, 0);
+    sim.start();
+    sim.pause(0.1);
+    titan::Mass *b = sim.createMass(Vec(0, 0, 10));
+    titan::Spring *s = sim.createSpring(a, b);
+    s->_k = 0;
+    sim.resume();
+    sim.pause(0.2);
+    sim.getAll();
+    EXPECT_NEAR(a->pos[0], sim.steps() * 0.0001, 1e-12);
+    EXPECT_NEAR(b->pos[2], 10, 0.0);
+    EXPECT_TRUE(sim.masses.size() == 2 && sim.springs.size() == 1);
+    sim.stop();
+}
+
+int main(int argc, char **argv) {
+    std::map<std::string, void (*)()> tests = {
+        {"simple_test", simple_test},         {"energy_test", energy_test},
+        {"external_test", external_test},     {"external_acc_test", external_acc_test},
+        {"multiagent_test", multiagent_test}, {"rotate_test", rotate_test},
+        {"breakpoint_and_step_test", breakpoint_and_step_test},
+        {"beam_fixed_face_test", beam_fixed_face_test},
+        {"topology_edit_test", topology_edit_test},
+    };
+    if (argc < 2 || !tests.count(argv[1])) {
+        for (auto &kv : tests) std::printf("%s\n", kv.first.c_str());
+        return argc < 2 ? 0 : 2;
+    }
+    try {
+        tests[argv[1]]();
+    } catch (const std::exception &e) {
+        std::fprintf(stderr, "exception: %s\n", e.what());
+        return 3;
+    }
+    std::printf("%s: %s\n", argv[1], failures ? "FAILED" : "ok");
+    return failures ? 1 : 0;
+}

@@ -139,7 +139,9 @@ def validate(sc, P, heavy_threshold=96):
                 assert len(expect[g]) > heavy_threshold
             else:
                 off = int(P["warp_inc_off"][w0 + i // 32])
-                codes = P["inc"][off + (i % 32) + 32 * np.arange(d)]
+                assert off % 128 == 0  # 8-byte aligned groups of four codes
+                j = np.arange(d)
+                codes = P["inc"][off + (j // 4) * 128 + 4 * (i % 32) + (j % 4)]
             got = [(int(sp[c & 0x7FFF]), -1 if c & 0x8000 else 1) for c in codes.tolist()]
             assert got == expect[g], (t, i)
     assert heavy_seen == sum(1 for e in expect if len(e) > heavy_threshold)

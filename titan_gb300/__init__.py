@@ -60,6 +60,7 @@ _SIGS = {
     "titan_gb300_set_body_plane": (ctypes.c_int, [_P, ctypes.c_int64, _D, ctypes.c_double, ctypes.c_double,
                                                   ctypes.c_double]),
     "titan_gb300_start": (ctypes.c_int, [_P, ctypes.c_int]),
+    "titan_gb300_set_launch": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "titan_gb300_synchronize": (ctypes.c_int, [_P]),
     "titan_gb300_time": (ctypes.c_double, [_P]),
@@ -244,6 +245,9 @@ class Sim:
                                                        friction_s), "set_body_plane")
 
     # -- device --
+    def set_launch(self, threads_per_cta: int):
+        self._check(self._L.titan_gb300_set_launch(self._h, threads_per_cta), "set_launch")
+
     def start(self, tile_masses: int = 0):
         self._check(self._L.titan_gb300_start(self._h, tile_masses), "start")
 

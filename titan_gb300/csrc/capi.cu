@@ -104,7 +104,8 @@ struct titan_gb300_sim {
     double *d_sk = nullptr, *d_srest = nullptr, *d_partials = nullptr, *d_dout = nullptr;
 
     size_t rsize() const { return prec == P_FP64 ? sizeof(double) : sizeof(float); }
-    int comps() const { return prec == P_FP32C ? 12 : 6; }
+    int comps() const { return tg::state_words(prec); }
+    int threads_req = 0;  // CTA size override (0: derived from the tile size)
 
     int fail(int code, const std::string &msg) {
         err = msg;
@@ -310,15 +311,17 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 256 : 512);
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : 256);
     in.heavy_threshold = 96;
-    // shared-memory budget: slab entries must fit beside the staged state
-    const size_t budget = 220 * 1024;
-    const size_t rs = s->rsize();
-    const int state_words = s->prec == P_FP32C ? 9 : 6;
-    in.slot_cap = std::min<int>(4095, std::max<int>(1024, in.tile_cap * 4));
-    long ecap = (long)((budget - (size_t)in.slot_cap * state_words * rs) / (3 * rs)) - 3 * 64;
-    in.entry_cap = (int)std::min<long>(32767, std::max<long>(ecap, 64));
+    // a tile's staged state, entry forces and heavy sums share one CTA's
+    // shared memory (tile_smem_bytes)
+    const int rs = (int)s->rsize();
+    in.slot_cap = 4095;
+    in.entry_cap = 32767;
+    in.smem_budget = 220 * 1024;
+    in.slot_bytes = (s->prec == P_FP32C ? 9 : 6) * rs;
+    in.entry_bytes = 3 * rs;
+    in.heavy_bytes = 3 * rs;
     return in;
 }
 
@@ -331,8 +334,7 @@ int build_device(titan_gb300_sim *s) {
     std::string why = tg::build_plan(in, s->plan);
     if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
     const tg::Plan &P = s->plan;
-    s->threads = std::max(32, std::min(512, ((P.max_nm + 31) / 32) * 32));
-    if (s->threads < 128) s->threads = 128;
+    s->threads = s->threads_req > 0 ? s->threads_req : std::max(128, std::min(512, ((P.max_nm + 31) / 32) * 32));
     s->npad = ((s->n + 127) / 128) * 128;
     const int64_t np = s->npad;
     auto &a = s->args;
@@ -341,7 +343,13 @@ int build_device(titan_gb300_sim *s) {
     a.slots = std::max(P.max_slots, 1);
     a.ecap = std::max(P.max_entries, 1);
     a.hcap = std::max(P.max_heavy, 1);
-    s->smem = tg::step_smem_bytes(s->prec, a.slots, a.ecap, P.max_heavy > 0 ? a.hcap : 0);
+    s->smem = 0;
+    for (int64_t t = 0; t < P.ntiles; t++) {
+        int slots = (int)(P.tile_mass_off[t + 1] - P.tile_mass_off[t] + P.tile_halo_off[t + 1] - P.tile_halo_off[t]);
+        int ne = (int)(P.tile_ent_off[t + 1] - P.tile_ent_off[t]);
+        int nh = (int)(P.tile_heavy_off[t + 1] - P.tile_heavy_off[t]);
+        s->smem = std::max(s->smem, tg::tile_smem_bytes(s->prec, slots, ne, nh));
+    }
     if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
     CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
 
@@ -534,6 +542,15 @@ void titan_gb300_destroy(titan_gb300_sim *s) {
     if (!s) return;
     if (s->stream) ensure_device(s);
     delete s;
+}
+
+int titan_gb300_set_launch(titan_gb300_sim *s, int threads_per_cta) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (threads_per_cta != 0 && (threads_per_cta < 64 || threads_per_cta > 512 || threads_per_cta % 32))
+        return s->fail(TITAN_GB300_EINVAL, "threads per CTA must be 0 or a multiple of 32 in [64, 512]");
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "set the launch shape before start");
+    s->threads_req = threads_per_cta;
+    return TITAN_GB300_OK;
 }
 
 int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
@@ -908,6 +925,7 @@ int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t 
         x.state0 = s->args.state0;
         x.state1 = s->args.state1;
         x.acc = s->args.acc;
+        x.parity = s->parity;
         if (idx) {
             CK(cudaMemcpyAsync(s->d_idx, idx, count * 8, cudaMemcpyHostToDevice, s->stream), "upload index");
             x.idx = s->d_idx;
@@ -1066,7 +1084,7 @@ int titan_gb300_plan_info(const titan_gb300_sim *s, int64_t out[12]) {
     // incidence word, 4 B per halo index, tile table.
     const int64_t rs = (int64_t)s->rsize();
     const int64_t comps = s->comps();
-    int64_t impl = s->n * (comps * rs * 2 + rs + 1 + 1);
+    int64_t impl = s->n * (comps * rs * 2 + rs + 1 + 1) + (int64_t)P.halo.size() * (f64 ? 48 : 36);
     impl += (int64_t)P.ent_ends.size() * (f64 ? 32 : 16) + nact_ent * (f64 ? 32 : 16);
     impl += (int64_t)P.inc.size() * 2 + (int64_t)P.heavy_inc.size() * 2 + (int64_t)P.halo.size() * 4;
     impl += P.ntiles * (int64_t)sizeof(tg::TileInfo);

@@ -102,7 +102,10 @@ struct DiagArgs {
 constexpr int kDiagBlocks = 512;
 constexpr int kDiagQ = 9;
 
-size_t step_smem_bytes(int precision, int slots, int ecap, int hcap);
+// words (of the precision's scalar) in one mass's state record
+int state_words(int precision);
+// dynamic shared memory of one tile's CTA
+size_t tile_smem_bytes(int precision, int slots, int entries, int heavy);
 cudaError_t step_prepare(int precision, size_t smem);
 cudaError_t launch_step(int precision, const StepArgs &a, int ntiles, int threads, size_t smem,
                         int parity, int write_acc, cudaStream_t s);

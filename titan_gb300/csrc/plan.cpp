@@ -162,6 +162,12 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                                 halo.push_back(x);
                             }
                 fits = nm + (int64_t)halo.size() <= in.slot_cap;
+                if (fits) {
+                    int64_t heavy = 0;
+                    for (int64_t m = lo; m < hi; m++) heavy += (ip[m + 1] - ip[m]) > in.heavy_threshold;
+                    fits = (nm + (int64_t)halo.size()) * in.slot_bytes + ne * in.entry_bytes +
+                               heavy * in.heavy_bytes <= in.smem_budget;
+                }
             }
             if (!fits) {
                 if (nm == 1)
@@ -201,6 +207,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     int64_t d = ip[m + 1] - ip[m];
                     if (d <= in.heavy_threshold) width = std::max(width, d);
                 }
+                width = (width + 3) & ~int64_t(3);
                 if (P.inc.size() > 0xffffffffULL - (uint64_t)(width * 32))
                     return "incidence table exceeds 2^32 words";
                 uint32_t off = (uint32_t)P.inc.size();
@@ -214,7 +221,8 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     };
                     if (d <= in.heavy_threshold) {
                         P.deg[m] = (uint8_t)d;
-                        for (int64_t j = 0; j < d; j++) P.inc[off + j * 32 + lane] = code_of(ip[m] + j);
+                        for (int64_t j = 0; j < d; j++)
+                            P.inc[ell_index(off, (uint32_t)lane, (uint32_t)j)] = code_of(ip[m] + j);
                     } else {
                         P.deg[m] = 255;
                         P.heavy_local.push_back((uint16_t)(m - lo));

@@ -29,7 +29,19 @@ struct PlanInput {
     int slot_cap = 4095;                 // tile + halo slots per tile (12-bit)
     int entry_cap = 32767;               // slab entries per tile (15-bit)
     int heavy_threshold = 96;            // degree above this: warp-cooperative
+    // shared-memory budget of one tile: slots * slot_bytes + entries *
+    // entry_bytes + heavy masses * heavy_bytes must not exceed smem_budget
+    int64_t smem_budget = 1 << 30;
+    int slot_bytes = 0, entry_bytes = 0, heavy_bytes = 0;
 };
+
+// Incidence words are stored four per lane: for the warp holding a mass at
+// lane l, code j of that mass is inc[warp_off + (j / 4) * 128 + 4 * l + j % 4],
+// so one 8-byte load fetches four codes and a warp's load is 256 contiguous
+// bytes.  A warp's block width is its largest degree rounded up to 4.
+inline uint64_t ell_index(uint64_t warp_off, uint32_t lane, uint32_t j) {
+    return warp_off + (uint64_t)(j >> 2) * 128 + 4 * lane + (j & 3);
+}
 
 // Entry word: left slot | right slot << 12 | type << 24 (slots are tile-local:
 // [0, nm) tile masses, [nm, nm+nh) halo masses).

@@ -12,190 +12,76 @@
 //      (src/sim.cu:1100-1166), and write the other ping-pong buffer.
 // The FP64 form is compiled without FMA contraction (build flag --fmad=false)
 // so that each operation is rounded as in the CPU oracle.
-#include "engine.h"
-
+//
+// State records (one per mass, tiled order), loaded with 16-byte vectors:
+//   FP64  48 B: x0 x1 | x2 v0 | v1 v2                (3 x double2)
+//   FP32C 48 B: xh0 xh1 xh2 vh0 | vh1 vh2 xl0 xl1 | xl2 vl0 vl1 vl2  (3 x float4)
+//   FP32  32 B: x0 x1 x2 v0 | v1 v2 - -              (2 x float4)
 #include <cstdint>
-#include <type_traits>
+
+#include "engine.h"
+#include "step_math.cuh"
 
 namespace tg {
 
 namespace {
 
-constexpr double kNormal = 20000.0;  // src/object.cu:26
+constexpr int kBatchB = 4;  // slab entries in flight per thread (phase B)
+constexpr int kBatchC = 4;  // 8-byte incidence words in flight per thread (phase C)
 
-// ---------------------------------------------------------------- FP64 ----
-__device__ __forceinline__ double nrm3(double a, double b, double c) {
-    return sqrt((a * a + b * b) + c * c);
-}
-__device__ __forceinline__ double dot3(const double *a, const double *b) {
-    return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
-}
+// ------------------------------------------------------- state records ----
+template <int PREC>
+struct St {
+    float x[3], v[3], xl[3], vl[3];
+};
+template <>
+struct St<P_FP64> {
+    double x[3], v[3], xl[3], vl[3];
+};
 
-// src/object.cu:73-106
-__device__ __forceinline__ void plane_apply(const double *n, double off, double fk, double fs,
-                                            const double *x, const double *v, double *F) {
-    double disp = dot3(x, n) - off;
-    if (!(disp < 0)) return;  // only zeros would be added otherwise
-    double fdn = dot3(F, n);
-    double fn[3] = {n[0] * fdn, n[1] * fdn, n[2] * fdn};
-    if (fs > 0 || fk > 0) {
-        double vdn = dot3(v, n);
-        double vp[3] = {v[0] - n[0] * vdn, v[1] - n[1] * vdn, v[2] - n[2] * vdn};
-        double vn = nrm3(vp[0], vp[1], vp[2]);
-        if (vn > 1e-16) {
-            double fmag = fk * nrm3(fn[0], fn[1], fn[2]);
-            F[0] = F[0] - (vp[0] * fmag) / vn;
-            F[1] = F[1] - (vp[1] * fmag) / vn;
-            F[2] = F[2] - (vp[2] * fmag) / vn;
-        } else {
-            double fp[3] = {F[0] - fn[0], F[1] - fn[1], F[2] - fn[2]};
-            if (fs * nrm3(fn[0], fn[1], fn[2]) > nrm3(fp[0], fp[1], fp[2])) {
-                F[0] = F[0] - fp[0];
-                F[1] = F[1] - fp[1];
-                F[2] = F[2] - fp[2];
-            }
-        }
+template <int PREC>
+__device__ __forceinline__ St<PREC> load_state(const void *buf, int64_t g) {
+    St<PREC> s;
+    if constexpr (PREC == P_FP64) {
+        const double2 *p = reinterpret_cast<const double2 *>(buf) + 3 * g;
+        double2 a0 = __ldg(p), a1 = __ldg(p + 1), a2 = __ldg(p + 2);
+        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a1.x;
+        s.v[0] = a1.y; s.v[1] = a2.x; s.v[2] = a2.y;
+    } else if constexpr (PREC == P_FP32C) {
+        const float4 *p = reinterpret_cast<const float4 *>(buf) + 3 * g;
+        float4 a0 = __ldg(p), a1 = __ldg(p + 1), a2 = __ldg(p + 2);
+        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a0.z;
+        s.v[0] = a0.w; s.v[1] = a1.x; s.v[2] = a1.y;
+        s.xl[0] = a1.z; s.xl[1] = a1.w; s.xl[2] = a2.x;
+        s.vl[0] = a2.y; s.vl[1] = a2.z; s.vl[2] = a2.w;
+    } else {
+        const float4 *p = reinterpret_cast<const float4 *>(buf) + 2 * g;
+        float4 a0 = __ldg(p);
+        float2 a1 = __ldg(reinterpret_cast<const float2 *>(p + 1));
+        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a0.z;
+        s.v[0] = a0.w; s.v[1] = a1.x; s.v[2] = a1.y;
     }
-    double s = (-disp) * kNormal;
-    F[0] = F[0] + n[0] * s;
-    F[1] = F[1] + n[1] * s;
-    F[2] = F[2] + n[2] * s;
-}
-
-// src/object.cu:53-56
-__device__ __forceinline__ void ball_apply(const double *c, double r, const double *x, double *F) {
-    double d[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
-    double dist = nrm3(d[0], d[1], d[2]);
-    if (dist <= r) {
-        F[0] = F[0] + (kNormal * d[0]) / dist;
-        F[1] = F[1] + (kNormal * d[1]) / dist;
-        F[2] = F[2] + (kNormal * d[2]) / dist;
-    }
-}
-
-// src/object.cu:115-124
-__device__ __forceinline__ void cplane_apply(const double *n, double fr, double *v, double *F) {
-    double nf = dot3(F, n);
-    F[0] = F[0] + (-n[0]) * nf;
-    F[1] = F[1] + (-n[1]) * nf;
-    F[2] = F[2] + (-n[2]) * nf;
-    double vn = nrm3(v[0], v[1], v[2]);
-    if (vn >= 1e-16) {
-        double vdn = dot3(v, n);
-        v[0] = v[0] + (-n[0]) * vdn;
-        v[1] = v[1] + (-n[1]) * vdn;
-        v[2] = v[2] + (-n[2]) * vdn;
-        double s = (-fr) * nf;
-        F[0] = F[0] + (v[0] * s) / vn;
-        F[1] = F[1] + (v[1] * s) / vn;
-        F[2] = F[2] + (v[2] * s) / vn;
-    }
-}
-
-// src/object.cu:133-141
-__device__ __forceinline__ void direction_apply(const double *t, double fr, double *v, double *F) {
-    double fdt = dot3(F, t);
-    double nf[3] = {F[0] - t[0] * fdt, F[1] - t[1] * fdt, F[2] - t[2] * fdt};
-    F[0] = F[0] + (-nf[0]);
-    F[1] = F[1] + (-nf[1]);
-    F[2] = F[2] + (-nf[2]);
-    if (nrm3(v[0], v[1], v[2]) >= 1e-16) {
-        double vdt = dot3(v, t);
-        v[0] = t[0] * vdt;
-        v[1] = t[1] * vdt;
-        v[2] = t[2] * vdt;
-        double s = (-nrm3(nf[0], nf[1], nf[2])) * fr;
-        F[0] = F[0] + t[0] * s;
-        F[1] = F[1] + t[1] * s;
-        F[2] = F[2] + t[2] * s;
-    }
-}
-
-// Local constraints of one mass (src/sim.cu:1117-1131), records pre-sorted.
-__device__ __forceinline__ void local_apply(const StepArgs &a, int64_t g, double *x, double *v,
-                                            double *F) {
-    for (int32_t r = a.lc_ptr[g]; r < a.lc_ptr[g + 1]; r++) {
-        const double *rec = a.lc_rec + 4 * (int64_t)r;
-        switch (a.lc_type[r]) {
-            case 1: plane_apply(rec, rec[3], 0.0, 0.0, x, v, F); break;
-            case 2: ball_apply(rec, rec[3], x, F); break;
-            case 0: cplane_apply(rec, rec[3], v, F); break;
-            case 3: direction_apply(rec, rec[3], v, F); break;
-            default: break;
-        }
-    }
-}
-
-// ---------------------------------------------------------------- FP32 ----
-__device__ __forceinline__ float nrm3f(float a, float b, float c) {
-    return __fsqrt_rn(fmaf(c, c, fmaf(b, b, a * a)));
-}
-__device__ __forceinline__ float dot3f(const float *a, const float *b) {
-    return fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0]));
-}
-
-__device__ __forceinline__ void plane_applyf(const float *n, float disp, float fk, float fs,
-                                             const float *v, float *F) {
-    if (!(disp < 0.f)) return;
-    float fdn = dot3f(F, n);
-    float fn[3] = {n[0] * fdn, n[1] * fdn, n[2] * fdn};
-    if (fs > 0.f || fk > 0.f) {
-        float vdn = dot3f(v, n);
-        float vp[3] = {v[0] - n[0] * vdn, v[1] - n[1] * vdn, v[2] - n[2] * vdn};
-        float vn = nrm3f(vp[0], vp[1], vp[2]);
-        if (vn > 1e-16f) {
-            float fm = __fdiv_rn(fk * nrm3f(fn[0], fn[1], fn[2]), vn);
-            F[0] -= vp[0] * fm;
-            F[1] -= vp[1] * fm;
-            F[2] -= vp[2] * fm;
-        } else {
-            float fp[3] = {F[0] - fn[0], F[1] - fn[1], F[2] - fn[2]};
-            if (fs * nrm3f(fn[0], fn[1], fn[2]) > nrm3f(fp[0], fp[1], fp[2])) {
-                F[0] -= fp[0];
-                F[1] -= fp[1];
-                F[2] -= fp[2];
-            }
-        }
-    }
-    float s = (-disp) * 20000.0f;
-    F[0] += n[0] * s;
-    F[1] += n[1] * s;
-    F[2] += n[2] * s;
-}
-
-__device__ __forceinline__ void ball_applyf(const float *d, float r, float *F) {
-    float dist = nrm3f(d[0], d[1], d[2]);
-    if (dist <= r) {
-        float s = __fdiv_rn(20000.0f, dist);
-        F[0] += d[0] * s;
-        F[1] += d[1] * s;
-        F[2] += d[2] * s;
-    }
-}
-
-// error-free transformations (Knuth two-sum, Dekker fast-two-sum)
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
-}
-
-// 32-byte record as two read-only 16-byte loads
-struct D4 { double x, y, z, w; };
-__device__ __forceinline__ D4 ldg_d4(const double *p) {
-    double2 a = __ldg(reinterpret_cast<const double2 *>(p));
-    double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-    return D4{a.x, a.y, b.x, b.y};
+    return s;
 }
 
 template <int PREC>
-struct Real { using T = float; };
-template <>
-struct Real<P_FP64> { using T = double; };
+__device__ __forceinline__ void store_state(void *buf, int64_t g, const St<PREC> &s) {
+    if constexpr (PREC == P_FP64) {
+        double2 *p = reinterpret_cast<double2 *>(buf) + 3 * g;
+        p[0] = make_double2(s.x[0], s.x[1]);
+        p[1] = make_double2(s.x[2], s.v[0]);
+        p[2] = make_double2(s.v[1], s.v[2]);
+    } else if constexpr (PREC == P_FP32C) {
+        float4 *p = reinterpret_cast<float4 *>(buf) + 3 * g;
+        p[0] = make_float4(s.x[0], s.x[1], s.x[2], s.v[0]);
+        p[1] = make_float4(s.v[1], s.v[2], s.xl[0], s.xl[1]);
+        p[2] = make_float4(s.xl[2], s.vl[0], s.vl[1], s.vl[2]);
+    } else {
+        float4 *p = reinterpret_cast<float4 *>(buf) + 2 * g;
+        p[0] = make_float4(s.x[0], s.x[1], s.x[2], s.v[0]);
+        p[1] = make_float4(s.v[1], s.v[2], 0.f, 0.f);
+    }
+}
 
 // ------------------------------------------------------------- kernel -----
 template <int PREC>
@@ -203,27 +89,28 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
     using R = typename Real<PREC>::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const TileInfo ti = a.tiles[blockIdx.x];
-    const int S = a.slots, E = a.ecap;
+    const int S = ti.nm + ti.nh, E = ti.ne;
     R *sx = reinterpret_cast<R *>(smem_raw);  // 3*S positions (hi)
     R *sv = sx + 3 * S;                        // 3*S velocities (hi)
     R *sxl = sv + 3 * S;                       // 3*S position lo (FP32C only)
     R *sF = (PREC == P_FP32C) ? sxl + 3 * S : sxl;  // 3*E entry forces
-    R *sH = sF + 3 * E;                        // 3*hcap heavy-mass sums
-    const R *in = reinterpret_cast<const R *>(parity ? a.state1 : a.state0);
-    R *out = reinterpret_cast<R *>(parity ? a.state0 : a.state1);
+    R *sH = sF + 3 * E;                        // 3*nheavy heavy-mass sums
+    const void *in = parity ? a.state1 : a.state0;
+    void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
     const double T = a.tbuf[parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = T + prm->dt;
 
     // ---- A: stage tile + halo -------------------------------------------
-    for (int i = threadIdx.x; i < ti.nm + ti.nh; i += blockDim.x) {
-        int64_t g = i < ti.nm ? (int64_t)ti.mass_off + i : (int64_t)a.halo[ti.halo_off + i - ti.nm];
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        int64_t g = i < ti.nm ? (int64_t)ti.mass_off + i : (int64_t)__ldg(a.halo + ti.halo_off + i - ti.nm);
+        St<PREC> s = load_state<PREC>(in, g);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            sx[c * S + i] = in[c * np + g];
-            sv[c * S + i] = in[(3 + c) * np + g];
-            if (PREC == P_FP32C) sxl[c * S + i] = in[(6 + c) * np + g];
+            sx[c * S + i] = s.x[c];
+            sv[c * S + i] = s.v[c];
+            if constexpr (PREC == P_FP32C) sxl[c * S + i] = s.xl[c];
         }
     }
     __syncthreads();
@@ -232,67 +119,87 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
     if constexpr (PREC == P_FP64) {
         const double *ent = reinterpret_cast<const double *>(a.ent) + 4 * (int64_t)ti.ent_off;
         const double *act = reinterpret_cast<const double *>(a.act) + 4 * (int64_t)ti.ent_off;
-        for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
-            D4 r = ldg_d4(ent + 4 * e);
-            uint32_t ends = (uint32_t)__double_as_longlong(r.w);
-            int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
-            double scale = 1.0;
-            if (e < ti.nact) {
-                D4 q = ldg_d4(act + 4 * e);
-                double th = q.x * T;
-                th = th + q.z;
-                double s = q.y * sin(th);
-                scale = ((ends >> 24) & 3) == 2 ? 1.0 - s : 1.0 + s;
+        for (int e0 = threadIdx.x; e0 < E; e0 += kBatchB * blockDim.x) {
+            D4 r[kBatchB], q[kBatchB];
+#pragma unroll
+            for (int k = 0; k < kBatchB; k++) {
+                int e = e0 + k * blockDim.x;
+                if (e < E) r[k] = ldg_d4(ent + 4 * e);
+                if (e < ti.nact) q[k] = ldg_d4(act + 4 * e);
             }
-            double d0 = sx[sb] - sx[sa], d1 = sx[S + sb] - sx[S + sa], d2 = sx[2 * S + sb] - sx[2 * S + sa];
-            double nrm = nrm3(d0, d1, d2);
-            double u0 = d0 / nrm, u1 = d1 / nrm, u2 = d2 / nrm;
-            double fs = r.x * (r.y * scale - nrm);
-            double f0 = u0 * fs, f1 = u1 * fs, f2 = u2 * fs;
-            if (r.z != 0.0) {
-                double w0 = sv[sa] - sv[sb], w1 = sv[S + sa] - sv[S + sb], w2 = sv[2 * S + sa] - sv[2 * S + sb];
-                double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * r.z;
-                f0 = f0 + u0 * dd;
-                f1 = f1 + u1 * dd;
-                f2 = f2 + u2 * dd;
+#pragma unroll
+            for (int k = 0; k < kBatchB; k++) {
+                int e = e0 + k * blockDim.x;
+                if (e >= E) break;
+                uint32_t ends = (uint32_t)__double_as_longlong(r[k].w);
+                int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
+                double scale = 1.0;
+                if (e < ti.nact) {
+                    double th = q[k].x * T;
+                    th = th + q[k].z;
+                    double s = q[k].y * sin(th);
+                    scale = ((ends >> 24) & 3) == 2 ? 1.0 - s : 1.0 + s;
+                }
+                double d0 = sx[sb] - sx[sa], d1 = sx[S + sb] - sx[S + sa], d2 = sx[2 * S + sb] - sx[2 * S + sa];
+                double nrm = nrm3(d0, d1, d2);
+                double u0 = d0 / nrm, u1 = d1 / nrm, u2 = d2 / nrm;
+                double fs = r[k].x * (r[k].y * scale - nrm);
+                double f0 = u0 * fs, f1 = u1 * fs, f2 = u2 * fs;
+                if (r[k].z != 0.0) {
+                    double w0 = sv[sa] - sv[sb], w1 = sv[S + sa] - sv[S + sb], w2 = sv[2 * S + sa] - sv[2 * S + sb];
+                    double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * r[k].z;
+                    f0 = f0 + u0 * dd;
+                    f1 = f1 + u1 * dd;
+                    f2 = f2 + u2 * dd;
+                }
+                sF[e] = f0;
+                sF[E + e] = f1;
+                sF[2 * E + e] = f2;
             }
-            sF[e] = f0;
-            sF[E + e] = f1;
-            sF[2 * E + e] = f2;
         }
     } else {
         const float4 *ent = reinterpret_cast<const float4 *>(a.ent) + ti.ent_off;
         const float4 *act = reinterpret_cast<const float4 *>(a.act) + ti.ent_off;
         const float Thi = (float)T;
         const float Tlo = (float)(T - (double)Thi);
-        for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
-            float4 r = __ldg(ent + e);
-            uint32_t ends = __float_as_uint(r.x);
-            int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
-            float rs = r.z;
-            if (e < ti.nact) {
-                float4 q = __ldg(act + e);
-                float th = fmaf(q.x, Thi, fmaf(q.x, Tlo, q.z));
-                float s = q.y * sinf(th);
-                rs = r.z * (((ends >> 24) & 3) == 2 ? 1.0f - s : 1.0f + s);
+        for (int e0 = threadIdx.x; e0 < E; e0 += kBatchB * blockDim.x) {
+            float4 r[kBatchB], q[kBatchB];
+#pragma unroll
+            for (int k = 0; k < kBatchB; k++) {
+                int e = e0 + k * blockDim.x;
+                if (e < E) r[k] = __ldg(ent + e);
+                if (e < ti.nact) q[k] = __ldg(act + e);
             }
-            float d0 = sx[sb] - sx[sa], d1 = sx[S + sb] - sx[S + sa], d2 = sx[2 * S + sb] - sx[2 * S + sa];
-            if (PREC == P_FP32C) {
-                d0 += sxl[sb] - sxl[sa];
-                d1 += sxl[S + sb] - sxl[S + sa];
-                d2 += sxl[2 * S + sb] - sxl[2 * S + sa];
+#pragma unroll
+            for (int k = 0; k < kBatchB; k++) {
+                int e = e0 + k * blockDim.x;
+                if (e >= E) break;
+                uint32_t ends = __float_as_uint(r[k].x);
+                int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
+                float rs = r[k].z;
+                if (e < ti.nact) {
+                    float th = fmaf(q[k].x, Thi, fmaf(q[k].x, Tlo, q[k].z));
+                    float s = q[k].y * sinf(th);
+                    rs = r[k].z * (((ends >> 24) & 3) == 2 ? 1.0f - s : 1.0f + s);
+                }
+                float d0 = sx[sb] - sx[sa], d1 = sx[S + sb] - sx[S + sa], d2 = sx[2 * S + sb] - sx[2 * S + sa];
+                if constexpr (PREC == P_FP32C) {
+                    d0 += sxl[sb] - sxl[sa];
+                    d1 += sxl[S + sb] - sxl[S + sa];
+                    d2 += sxl[2 * S + sb] - sxl[2 * S + sa];
+                }
+                float nrm = nrm3f(d0, d1, d2);
+                float inv = __frcp_rn(nrm);
+                float u0 = d0 * inv, u1 = d1 * inv, u2 = d2 * inv;
+                float f = r[k].y * (rs - nrm);
+                if (r[k].w != 0.f) {
+                    float w0 = sv[sa] - sv[sb], w1 = sv[S + sa] - sv[S + sb], w2 = sv[2 * S + sa] - sv[2 * S + sb];
+                    f = fmaf(fmaf(w2, u2, fmaf(w1, u1, w0 * u0)), r[k].w, f);
+                }
+                sF[e] = u0 * f;
+                sF[E + e] = u1 * f;
+                sF[2 * E + e] = u2 * f;
             }
-            float nrm = nrm3f(d0, d1, d2);
-            float inv = __frcp_rn(nrm);
-            float u0 = d0 * inv, u1 = d1 * inv, u2 = d2 * inv;
-            float f = r.y * (rs - nrm);
-            if (r.w != 0.f) {
-                float w0 = sv[sa] - sv[sb], w1 = sv[S + sa] - sv[S + sb], w2 = sv[2 * S + sa] - sv[2 * S + sb];
-                f = fmaf(fmaf(w2, u2, fmaf(w1, u1, w0 * u0)), r.w, f);
-            }
-            sF[e] = u0 * f;
-            sF[E + e] = u1 * f;
-            sF[2 * E + e] = u2 * f;
         }
     }
     __syncthreads();
@@ -325,8 +232,8 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             }
             if (lane == 0) {
                 sH[h] = p0;
-                sH[a.hcap + h] = p1;
-                sH[2 * a.hcap + h] = p2;
+                sH[ti.nheavy + h] = p1;
+                sH[2 * ti.nheavy + h] = p2;
             }
         }
         __syncthreads();
@@ -335,37 +242,57 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
     // ---- C: per-mass gather, constraints, integration ----------------------
     for (int i = threadIdx.x; i < ti.nm; i += blockDim.x) {
         const int64_t g = (int64_t)ti.mass_off + i;
-        const uint8_t fl = a.flags[g];
+        const uint8_t fl = __ldg(a.flags + g);
         if (fl & MF_FIXED) continue;  // src/sim.cu:1100
-        const uint32_t d = a.deg[g];
-        R F[3] = {0, 0, 0};
+        const uint32_t d = __ldg(a.deg + g);
+        const R m = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+        R F0 = 0, F1 = 0, F2 = 0;
         if (d == 255) {
             int h = 0;
             while (h < ti.nheavy && a.heavy_local[ti.heavy_off + h] != i) h++;
-            F[0] = F[0] + sH[h];
-            F[1] = F[1] + sH[a.hcap + h];
-            F[2] = F[2] + sH[2 * a.hcap + h];
+            F0 = F0 + sH[h];
+            F1 = F1 + sH[ti.nheavy + h];
+            F2 = F2 + sH[2 * ti.nheavy + h];
         } else if (d > 0) {
-            const uint16_t *ip = a.inc + a.warp_inc_off[ti.warp_off + (i >> 5)] + (i & 31);
-            for (uint32_t j = 0; j < d; j++) {
-                uint32_t code = __ldg(ip + 32 * j);
-                int idx = code & 0x7fff;
-                if (code & 0x8000) {
-                    F[0] = F[0] + (-sF[idx]);
-                    F[1] = F[1] + (-sF[E + idx]);
-                    F[2] = F[2] + (-sF[2 * E + idx]);
-                } else {
-                    F[0] = F[0] + sF[idx];
-                    F[1] = F[1] + sF[E + idx];
-                    F[2] = F[2] + sF[2 * E + idx];
+            const uint2 *ip =
+                reinterpret_cast<const uint2 *>(a.inc + a.warp_inc_off[ti.warp_off + (i >> 5)]) + (i & 31);
+            const uint32_t nw = (d + 3) >> 2;
+            for (uint32_t w0 = 0; w0 < nw; w0 += kBatchC) {
+                uint2 cw[kBatchC];
+#pragma unroll
+                for (int k = 0; k < kBatchC; k++)
+                    if (w0 + k < nw) cw[k] = __ldg(ip + 32 * (w0 + k));
+#pragma unroll
+                for (int k = 0; k < kBatchC; k++) {
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        const uint32_t j = 4 * (w0 + k) + h;
+                        if (j < d) {
+                            const uint32_t word = h < 2 ? cw[k].x : cw[k].y;
+                            const uint32_t code = (word >> (16 * (h & 1))) & 0xffffu;
+                            const int idx = code & 0x7fff;
+                            if (code & 0x8000) {
+                                F0 = F0 + (-sF[idx]);
+                                F1 = F1 + (-sF[E + idx]);
+                                F2 = F2 + (-sF[2 * E + idx]);
+                            } else {
+                                F0 = F0 + sF[idx];
+                                F1 = F1 + sF[E + idx];
+                                F2 = F2 + sF[2 * E + idx];
+                            }
+                        }
+                    }
                 }
             }
         }
+        St<PREC> s;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            s.x[c] = sx[c * S + i];
+            s.v[c] = sv[c * S + i];
+        }
         if constexpr (PREC == P_FP64) {
-            const double m = reinterpret_cast<const double *>(a.mass)[g];
-            double x[3] = {sx[i], sx[S + i], sx[2 * S + i]};
-            double v[3] = {sv[i], sv[S + i], sv[2 * S + i]};
-            double *Fd = reinterpret_cast<double *>(F);
+            double Fd[3] = {F0, F1, F2};
             Fd[0] = Fd[0] + prm->g[0] * m;
             Fd[1] = Fd[1] + prm->g[1] * m;
             Fd[2] = Fd[2] + prm->g[2] * m;
@@ -377,33 +304,31 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             }
             for (int j = 0; j < prm->nplanes; j++) {
                 const double *p = prm->plane[j];
-                plane_apply(p, p[3], p[4], p[5], x, v, Fd);
+                plane_apply(p, p[3], p[4], p[5], s.x, s.v, Fd);
             }
-            for (int j = 0; j < prm->nballs; j++) ball_apply(prm->ball[j], prm->ball[j][3], x, Fd);
+            for (int j = 0; j < prm->nballs; j++) ball_apply(prm->ball[j], prm->ball[j][3], s.x, Fd);
             if (fl & MF_BODYPLANE) {
                 const double *p = a.body_plane + 6 * (int64_t)ti.body;
-                plane_apply(p, p[3], p[4], p[5], x, v, Fd);
+                plane_apply(p, p[3], p[4], p[5], s.x, s.v, Fd);
             }
-            if (fl & MF_LOCAL) local_apply(a, g, x, v, Fd);
+            if (fl & MF_LOCAL) local_apply(a, g, s.x, s.v, Fd);
             if (fl & MF_DRAG) {  // src/sim.cu:1134-1137
-                double vn = nrm3(v[0], v[1], v[2]);
+                double vn = nrm3(s.v[0], s.v[1], s.v[2]);
                 if (vn != 0.0) {
                     double c = (double)(-a.drag[g]) * (vn * vn);
-                    Fd[0] = Fd[0] + (v[0] * c) / vn;
-                    Fd[1] = Fd[1] + (v[1] * c) / vn;
-                    Fd[2] = Fd[2] + (v[2] * c) / vn;
+                    Fd[0] = Fd[0] + (s.v[0] * c) / vn;
+                    Fd[1] = Fd[1] + (s.v[1] * c) / vn;
+                    Fd[2] = Fd[2] + (s.v[2] * c) / vn;
                 }
             }
             const double dt = prm->dt;
             double acc[3] = {Fd[0] / m, Fd[1] / m, Fd[2] / m};
-            double *o = reinterpret_cast<double *>(out);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                v[c] = v[c] + acc[c] * dt;
-                x[c] = x[c] + v[c] * dt;
-                o[c * np + g] = x[c];
-                o[(3 + c) * np + g] = v[c];
+                s.v[c] = s.v[c] + acc[c] * dt;
+                s.x[c] = s.x[c] + s.v[c] * dt;
             }
+            store_state<PREC>(out, g, s);
             if (write_acc) {
                 double *ac = reinterpret_cast<double *>(a.acc);
                 ac[g] = acc[0];
@@ -411,54 +336,48 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
                 ac[2 * np + g] = acc[2];
             }
         } else {
-            float *Ff = reinterpret_cast<float *>(F);
-            const float m = reinterpret_cast<const float *>(a.mass)[g];
-            float xh[3] = {(float)sx[i], (float)sx[S + i], (float)sx[2 * S + i]};
-            float xl[3] = {0.f, 0.f, 0.f};
-            float vh[3] = {(float)sv[i], (float)sv[S + i], (float)sv[2 * S + i]};
-            float vl[3] = {0.f, 0.f, 0.f};
-            const float *inf = reinterpret_cast<const float *>(in);
-            if (PREC == P_FP32C) {
+            if constexpr (PREC == P_FP32C) {
+                const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    xl[c] = (float)sxl[c * S + i];
-                    vl[c] = inf[(9 + c) * np + g];
-                }
+                for (int c = 0; c < 3; c++) s.xl[c] = sxl[c * S + i];
+                s.vl[0] = a2.y;
+                s.vl[1] = a2.z;
+                s.vl[2] = a2.w;
+            } else {
+#pragma unroll
+                for (int c = 0; c < 3; c++) s.xl[c] = s.vl[c] = 0.f;
             }
-            Ff[0] = fmaf(prm->gf[0], m, Ff[0]);
-            Ff[1] = fmaf(prm->gf[1], m, Ff[1]);
-            Ff[2] = fmaf(prm->gf[2], m, Ff[2]);
+            float Ff[3] = {fmaf(prm->gf[0], m, F0), fmaf(prm->gf[1], m, F1), fmaf(prm->gf[2], m, F2)};
             if (fl & MF_EXT) {
                 const float *ext = reinterpret_cast<const float *>(a.ext);
                 Ff[0] += ext[g];
                 Ff[1] += ext[np + g];
                 Ff[2] += ext[2 * np + g];
             }
-            float vv[3] = {vh[0] + vl[0], vh[1] + vl[1], vh[2] + vl[2]};
+            float vv[3] = {s.v[0] + s.vl[0], s.v[1] + s.vl[1], s.v[2] + s.vl[2]};
             for (int j = 0; j < prm->nplanes; j++) {
                 const float *p = prm->planef[j];
-                float disp = (dot3f(xh, p) - p[3]) + dot3f(xl, p);
+                float disp = (dot3f(s.x, p) - p[3]) + dot3f(s.xl, p);
                 plane_applyf(p, disp, p[4], p[5], vv, Ff);
             }
             for (int j = 0; j < prm->nballs; j++) {
                 const float *b = prm->ballf[j];
-                float dd[3] = {(xh[0] - b[0]) + xl[0], (xh[1] - b[1]) + xl[1], (xh[2] - b[2]) + xl[2]};
+                float dd[3] = {(s.x[0] - b[0]) + s.xl[0], (s.x[1] - b[1]) + s.xl[1], (s.x[2] - b[2]) + s.xl[2]};
                 ball_applyf(dd, b[3], Ff);
             }
             if (fl & MF_BODYPLANE) {
                 const float *p = a.body_planef + 6 * (int64_t)ti.body;
-                float disp = (dot3f(xh, p) - p[3]) + dot3f(xl, p);
+                float disp = (dot3f(s.x, p) - p[3]) + dot3f(s.xl, p);
                 plane_applyf(p, disp, p[4], p[5], vv, Ff);
             }
             if (fl & (MF_LOCAL | MF_DRAG)) {
                 // rare paths: evaluate in FP64 on the compensated values
-                double x[3], v[3], Fd[3];
+                double x[3], v[3], Fd[3], v0[3];
                 for (int c = 0; c < 3; c++) {
-                    x[c] = (double)xh[c] + (double)xl[c];
-                    v[c] = (double)vh[c] + (double)vl[c];
+                    x[c] = (double)s.x[c] + (double)s.xl[c];
+                    v0[c] = v[c] = (double)s.v[c] + (double)s.vl[c];
                     Fd[c] = Ff[c];
                 }
-                double v0[3] = {v[0], v[1], v[2]};
                 if (fl & MF_LOCAL) local_apply(a, g, x, v, Fd);
                 if (fl & MF_DRAG) {
                     double vn = nrm3(v[0], v[1], v[2]);
@@ -470,42 +389,36 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
                 for (int c = 0; c < 3; c++) {
                     Ff[c] = (float)Fd[c];
                     if (v[c] != v0[c]) {  // a constraint projected the velocity
-                        vh[c] = (float)v[c];
-                        vl[c] = (float)(v[c] - (double)vh[c]);
+                        s.v[c] = (float)v[c];
+                        s.vl[c] = (float)(v[c] - (double)s.v[c]);
                     }
                 }
             }
             const float inv_m = __frcp_rn(m);
             float acc[3];
-            float *o = reinterpret_cast<float *>(out);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 acc[c] = Ff[c] * inv_m;
-                if (PREC == P_FP32C) {
+                if constexpr (PREC == P_FP32C) {
                     // v += a dt with dt = dt_hi + dt_lo, compensated
                     float p = acc[c] * prm->dt_hi;
                     float pe = fmaf(acc[c], prm->dt_hi, -p) + acc[c] * prm->dt_lo;
-                    float s, e;
-                    two_sum(vh[c], p, s, e);
-                    e += vl[c] + pe;
-                    fast_two_sum(s, e, vh[c], vl[c]);
+                    float sum, err;
+                    two_sum(s.v[c], p, sum, err);
+                    err += s.vl[c] + pe;
+                    fast_two_sum(sum, err, s.v[c], s.vl[c]);
                     // x += v dt
-                    float q = vh[c] * prm->dt_hi;
-                    float qe = fmaf(vh[c], prm->dt_hi, -q) + fmaf(vh[c], prm->dt_lo, vl[c] * prm->dt_hi);
-                    two_sum(xh[c], q, s, e);
-                    e += xl[c] + qe;
-                    fast_two_sum(s, e, xh[c], xl[c]);
-                    o[c * np + g] = xh[c];
-                    o[(3 + c) * np + g] = vh[c];
-                    o[(6 + c) * np + g] = xl[c];
-                    o[(9 + c) * np + g] = vl[c];
+                    float q = s.v[c] * prm->dt_hi;
+                    float qe = fmaf(s.v[c], prm->dt_hi, -q) + fmaf(s.v[c], prm->dt_lo, s.vl[c] * prm->dt_hi);
+                    two_sum(s.x[c], q, sum, err);
+                    err += s.xl[c] + qe;
+                    fast_two_sum(sum, err, s.x[c], s.xl[c]);
                 } else {
-                    vh[c] = vh[c] + acc[c] * prm->dt_hi;
-                    xh[c] = xh[c] + vh[c] * prm->dt_hi;
-                    o[c * np + g] = xh[c];
-                    o[(3 + c) * np + g] = vh[c];
+                    s.v[c] = s.v[c] + acc[c] * prm->dt_hi;
+                    s.x[c] = s.x[c] + s.v[c] * prm->dt_hi;
                 }
             }
+            store_state<PREC>(out, g, s);
             if (write_acc) {
                 float *ac = reinterpret_cast<float *>(a.acc);
                 ac[g] = acc[0];
@@ -524,14 +437,14 @@ __global__ void k_gather(XferArgs a) {
     if (i >= a.count) return;
     int64_t src = a.idx ? a.idx[i] : i;
     int64_t g = a.old2new[src];
-    const R *st = reinterpret_cast<const R *>(a.parity ? a.state1 : a.state0);
+    const St<PREC> s = load_state<PREC>(a.parity ? a.state1 : a.state0, g);
     const int64_t np = a.npad;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        double x = (double)st[c * np + g], v = (double)st[(3 + c) * np + g];
-        if (PREC == P_FP32C) {
-            x += (double)st[(6 + c) * np + g];
-            v += (double)st[(9 + c) * np + g];
+        double x = (double)s.x[c], v = (double)s.v[c];
+        if constexpr (PREC == P_FP32C) {
+            x += (double)s.xl[c];
+            v += (double)s.vl[c];
         }
         if (a.pos) a.pos[3 * i + c] = x;
         if (a.vel) a.vel[3 * i + c] = v;
@@ -539,6 +452,8 @@ __global__ void k_gather(XferArgs a) {
     }
 }
 
+// Writes pos and/or vel of the listed masses into both buffers, keeping the
+// other field from the current buffer.
 template <int PREC>
 __global__ void k_scatter(XferArgs a) {
     using R = typename Real<PREC>::T;
@@ -547,26 +462,23 @@ __global__ void k_scatter(XferArgs a) {
     int64_t src = a.idx ? a.idx[i] : i;
     int64_t g = a.old2new[src];
     const int64_t np = a.npad;
-    R *bufs[2] = {reinterpret_cast<R *>(a.state0), reinterpret_cast<R *>(a.state1)};
+    St<PREC> s = load_state<PREC>(a.parity ? a.state1 : a.state0, g);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        for (int b = 0; b < 2; b++) {
-            R *st = bufs[b];
-            if (a.ipos) {
-                double x = a.ipos[3 * i + c];
-                R h = (R)x;
-                st[c * np + g] = h;
-                if (PREC == P_FP32C) st[(6 + c) * np + g] = (R)(x - (double)h);
-            }
-            if (a.ivel) {
-                double v = a.ivel[3 * i + c];
-                R h = (R)v;
-                st[(3 + c) * np + g] = h;
-                if (PREC == P_FP32C) st[(9 + c) * np + g] = (R)(v - (double)h);
-            }
+        if (a.ipos) {
+            double x = a.ipos[3 * i + c];
+            s.x[c] = (R)x;
+            if constexpr (PREC == P_FP32C) s.xl[c] = (R)(x - (double)s.x[c]);
+        }
+        if (a.ivel) {
+            double v = a.ivel[3 * i + c];
+            s.v[c] = (R)v;
+            if constexpr (PREC == P_FP32C) s.vl[c] = (R)(v - (double)s.v[c]);
         }
         if (a.ipos) reinterpret_cast<R *>(a.acc)[c * np + g] = (R)0;
     }
+    store_state<PREC>(a.state0, g, s);
+    store_state<PREC>(a.state1, g, s);
 }
 
 // ------------------------------------------------------ diagnostics -------
@@ -574,29 +486,28 @@ __global__ void k_scatter(XferArgs a) {
 // and reduces it with a fixed tree; pass 2 reduces the partials the same way.
 template <int PREC>
 __global__ void __launch_bounds__(256) k_diag1(DiagArgs a) {
-    using R = typename Real<PREC>::T;
     __shared__ double red[kDiagQ][256];
     double q[kDiagQ];
 #pragma unroll
     for (int k = 0; k < kDiagQ; k++) q[k] = 0.0;
-    const R *st = reinterpret_cast<const R *>(a.state);
+    using R = typename Real<PREC>::T;
     const R *ms = reinterpret_cast<const R *>(a.mass);
-    const int64_t np = a.npad;
-    auto pos = [&](int64_t g, int c) {
-        double x = (double)st[c * np + g];
-        if (PREC == P_FP32C) x += (double)st[(6 + c) * np + g];
+    auto pos = [&](const St<PREC> &s, int c) {
+        double x = (double)s.x[c];
+        if constexpr (PREC == P_FP32C) x += (double)s.xl[c];
         return x;
     };
-    auto vel = [&](int64_t g, int c) {
-        double v = (double)st[(3 + c) * np + g];
-        if (PREC == P_FP32C) v += (double)st[(9 + c) * np + g];
+    auto vel = [&](const St<PREC> &s, int c) {
+        double v = (double)s.v[c];
+        if constexpr (PREC == P_FP32C) v += (double)s.vl[c];
         return v;
     };
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.n; g += stride) {
+        const St<PREC> s = load_state<PREC>(a.state, g);
         double m = (double)ms[g];
-        double x[3] = {pos(g, 0), pos(g, 1), pos(g, 2)};
-        double v[3] = {vel(g, 0), vel(g, 1), vel(g, 2)};
+        double x[3] = {pos(s, 0), pos(s, 1), pos(s, 2)};
+        double v[3] = {vel(s, 0), vel(s, 1), vel(s, 2)};
         double vn = nrm3(v[0], v[1], v[2]);
         q[1] += (0.5 * m) * (vn * vn);
         q[2] += (a.g_mag * x[2]) * m;
@@ -611,7 +522,8 @@ __global__ void __launch_bounds__(256) k_diag1(DiagArgs a) {
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < a.ns; s += stride) {
         int32_t l = a.sl[s], r = a.sr[s];
         if (l < 0) continue;
-        double d0 = pos(l, 0) - pos(r, 0), d1 = pos(l, 1) - pos(r, 1), d2 = pos(l, 2) - pos(r, 2);
+        const St<PREC> sl = load_state<PREC>(a.state, l), sr = load_state<PREC>(a.state, r);
+        double d0 = pos(sl, 0) - pos(sr, 0), d1 = pos(sl, 1) - pos(sr, 1), d2 = pos(sl, 2) - pos(sr, 2);
         double x = nrm3(d0, d1, d2) - a.srest[s];
         q[0] += (a.sk[s] * (x * x)) / 2;
     }
@@ -644,8 +556,10 @@ __global__ void __launch_bounds__(256) k_diag2(DiagArgs a) {
 
 }  // namespace
 
-size_t step_smem_bytes(int precision, int slots, int ecap, int hcap) {
-    size_t words = (size_t)(precision == P_FP32C ? 9 : 6) * slots + 3 * (size_t)ecap + 3 * (size_t)hcap;
+int state_words(int precision) { return precision == P_FP64 ? 6 : (precision == P_FP32C ? 12 : 8); }
+
+size_t tile_smem_bytes(int precision, int slots, int entries, int heavy) {
+    size_t words = (size_t)(precision == P_FP32C ? 9 : 6) * slots + 3 * (size_t)entries + 3 * (size_t)heavy;
     return words * (precision == P_FP64 ? sizeof(double) : sizeof(float));
 }
 

@@ -153,7 +153,7 @@ def config3(nbodies=4096, seed=3, side_range=(3, 12), spacing=0.1, pitch=2.0):
     return sc
 
 
-def load(sim: Sim, sc: dict, start=True, tile_masses=0):
+def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0):
     """Upload a scene into a Sim handle (and start it)."""
     sim.set_time_step(sc["dt"])
     sim.set_global_acc(sc["g"])
@@ -172,10 +172,12 @@ def load(sim: Sim, sc: dict, start=True, tile_masses=0):
         for b, (n, off, fk, fs) in enumerate(sc.get("body_planes", [])):
             if n is not None:
                 sim.set_body_plane(b, n, off, fk, fs)
+    if threads:
+        sim.set_launch(threads)
     if start:
         sim.start(tile_masses)
     return sim
 
 
-def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0) -> Sim:
-    return load(Sim(precision, device), sc, True, tile_masses)
+def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0) -> Sim:
+    return load(Sim(precision, device), sc, True, tile_masses, threads)
