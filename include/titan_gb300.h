@@ -143,6 +143,17 @@ int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
  * tile size itself is start()'s argument.  Used by the autotuner. */
 int titan_gb300_set_launch(titan_gb300_sim *sim, int threads_per_cta);
 
+/* Step kernel form: 0 = automatic (the pipelined persistent kernel whenever
+ * two of the scene's tiles fit in shared memory, else the per-tile kernel),
+ * 1 = per-tile kernel (one CTA per tile), 2 = pipelined kernel (fails at
+ * start() when the tiles are too large).  Both forms give bit-identical
+ * results.  Set before start(). */
+int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
+
+/* After start(): out[0] kernel form in use (1 or 2), out[1] CTAs per launch,
+ * out[2] threads per CTA, out[3] dynamic shared memory per CTA (bytes). */
+int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
+
 /* One iteration of the reference's execute() loop body (src/sim.cu:1569-1590)
  * nsteps times: spring forces + mass update fused into one kernel per step,
  * replayed from cached CUDA graphs.  Asynchronous. */
@@ -232,6 +243,7 @@ int64_t titan_gb300_plan_table(const titan_gb300_sim *sim, int table, void *out)
 #define TITAN_GB300_T_HEAVY_INC_OFF 14 /* uint32: nheavy+1                       */
 #define TITAN_GB300_T_HEAVY_INC 15     /* uint16                                 */
 #define TITAN_GB300_T_BODY_OF_TILE 16  /* int32                                  */
+#define TITAN_GB300_T_TILE_NH 17       /* int32: halo masses of each tile (HALO lists are padded to 4) */
 
 /* Lattice builder of createLattice (src/sim.cu:1923-1944, src/object.cu:232-293):
  * fills pos (3*nx*ny*nz) and, when non-NULL, left/right/rest of the

@@ -45,12 +45,12 @@ def test_create_needs_no_gpu_and_validates():
 T = {name: i for i, name in enumerate(
     ["new2old", "tile_mass_off", "tile_halo_off", "halo", "tile_ent_off", "tile_nact", "ent_ends", "ent_spring",
      "tile_warp_off", "warp_inc_off", "deg", "inc", "tile_heavy_off", "heavy_local", "heavy_inc_off", "heavy_inc",
-     "body_of_tile"])}
+     "body_of_tile", "tile_nh"])}
 DT = {"new2old": np.int32, "tile_mass_off": np.int64, "tile_halo_off": np.int64, "halo": np.int32,
       "tile_ent_off": np.int64, "tile_nact": np.int32, "ent_ends": np.uint32, "ent_spring": np.int64,
       "tile_warp_off": np.int64, "warp_inc_off": np.uint32, "deg": np.uint8, "inc": np.uint16,
       "tile_heavy_off": np.int64, "heavy_local": np.uint16, "heavy_inc_off": np.uint32, "heavy_inc": np.uint16,
-      "body_of_tile": np.int32}
+      "body_of_tile": np.int32, "tile_nh": np.int32}
 
 
 def plan_tables(sc, tile, precision=tg.FP32C):
@@ -106,7 +106,9 @@ def validate(sc, P, heavy_threshold=96):
     for t in range(ntiles):
         m0, m1 = tmo[t], tmo[t + 1]
         nm = m1 - m0
-        halo = P["halo"][P["tile_halo_off"][t]:P["tile_halo_off"][t + 1]]
+        h0 = P["tile_halo_off"][t]
+        assert h0 % 4 == 0 and P["tile_halo_off"][t + 1] - h0 == (P["tile_nh"][t] + 3) // 4 * 4
+        halo = P["halo"][h0:h0 + P["tile_nh"][t]]
         assert np.all(np.diff(halo) > 0)
         assert not np.any((halo >= m0) & (halo < m1))
         slot2g = np.concatenate([np.arange(m0, m1), halo])

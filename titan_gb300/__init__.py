@@ -61,6 +61,8 @@ _SIGS = {
                                                   ctypes.c_double]),
     "titan_gb300_start": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_launch": (ctypes.c_int, [_P, ctypes.c_int]),
+    "titan_gb300_set_kernel": (ctypes.c_int, [_P, ctypes.c_int]),
+    "titan_gb300_kernel_info": (ctypes.c_int, [_P, _I64]),
     "titan_gb300_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "titan_gb300_synchronize": (ctypes.c_int, [_P]),
     "titan_gb300_time": (ctypes.c_double, [_P]),
@@ -247,6 +249,16 @@ class Sim:
     # -- device --
     def set_launch(self, threads_per_cta: int):
         self._check(self._L.titan_gb300_set_launch(self._h, threads_per_cta), "set_launch")
+
+    def set_kernel(self, variant: int):
+        """0 automatic, 1 per-tile kernel, 2 pipelined persistent kernel."""
+        self._check(self._L.titan_gb300_set_kernel(self._h, variant), "set_kernel")
+
+    def kernel_info(self) -> dict:
+        out = np.zeros(4, np.int64)
+        self._check(self._L.titan_gb300_kernel_info(self._h, _ptr(out, ctypes.c_int64)), "kernel_info")
+        return {"kernel": "pipelined" if out[0] == 2 else "per-tile", "ctas": int(out[1]), "threads": int(out[2]),
+                "smem_bytes": int(out[3])}
 
     def start(self, tile_masses: int = 0):
         self._check(self._L.titan_gb300_start(self._h, tile_masses), "start")

@@ -34,7 +34,7 @@ NVCC_KERNEL_EXTRA = {"step.cu": ["--fmad=false"]}
 CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 
-LIB_CU = ["step.cu", "capi.cu"]
+LIB_CU = sorted(p.name for p in CSRC.glob("*.cu"))
 LIB_CPP = ["plan.cpp", "lattice.cpp"]
 SIM_CPP = ["simulation.cpp"]
 

@@ -106,6 +106,15 @@ struct titan_gb300_sim {
     size_t rsize() const { return prec == P_FP64 ? sizeof(double) : sizeof(float); }
     int comps() const { return tg::state_words(prec); }
     int threads_req = 0;  // CTA size override (0: derived from the tile size)
+    int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 2 pipelined kernel
+    bool use_pipe = false;
+    int ctas = 0;         // persistent grid of the pipelined kernel
+    int *d_err = nullptr;
+
+    cudaError_t launch(int parity, int write_acc) {
+        if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
+        return tg::launch_step(prec, args, (int)plan.ntiles, threads, smem, parity, write_acc, stream);
+    }
 
     int fail(int code, const std::string &msg) {
         err = msg;
@@ -311,7 +320,7 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : 256);
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 64 : 128);
     in.heavy_threshold = 96;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)
@@ -343,24 +352,16 @@ int build_device(titan_gb300_sim *s) {
     a.slots = std::max(P.max_slots, 1);
     a.ecap = std::max(P.max_entries, 1);
     a.hcap = std::max(P.max_heavy, 1);
-    s->smem = 0;
-    for (int64_t t = 0; t < P.ntiles; t++) {
-        int slots = (int)(P.tile_mass_off[t + 1] - P.tile_mass_off[t] + P.tile_halo_off[t + 1] - P.tile_halo_off[t]);
-        int ne = (int)(P.tile_ent_off[t + 1] - P.tile_ent_off[t]);
-        int nh = (int)(P.tile_heavy_off[t + 1] - P.tile_heavy_off[t]);
-        s->smem = std::max(s->smem, tg::tile_smem_bytes(s->prec, slots, ne, nh));
-    }
-    if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
-    CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
-
     cudaError_t e = cudaSuccess;
+    s->smem = 0;
+    int64_t max_ne = 0, max_nact = 0, max_incw = 0, max_nh = 0, max_slots = 0, max_heavy = 0;
     std::vector<tg::TileInfo> tiles(P.ntiles);
     for (int64_t t = 0; t < P.ntiles; t++) {
         tg::TileInfo &ti = tiles[t];
         ti.mass_off = (int32_t)P.tile_mass_off[t];
         ti.nm = (int32_t)(P.tile_mass_off[t + 1] - P.tile_mass_off[t]);
         ti.halo_off = (int32_t)P.tile_halo_off[t];
-        ti.nh = (int32_t)(P.tile_halo_off[t + 1] - P.tile_halo_off[t]);
+        ti.nh = P.tile_nh[t];
         ti.ent_off = (int32_t)P.tile_ent_off[t];
         ti.ne = (int32_t)(P.tile_ent_off[t + 1] - P.tile_ent_off[t]);
         ti.nact = P.tile_nact[t];
@@ -368,8 +369,54 @@ int build_device(titan_gb300_sim *s) {
         ti.heavy_off = (int32_t)P.tile_heavy_off[t];
         ti.nheavy = (int32_t)(P.tile_heavy_off[t + 1] - P.tile_heavy_off[t]);
         ti.body = P.body_of_tile[t];
-        ti.pad = 0;
+        const int64_t w0 = P.tile_warp_off[t], w1 = P.tile_warp_off[t + 1];
+        const int64_t i0 = w1 > w0 ? (int64_t)P.warp_inc_off[w0] : 0;
+        const int64_t i1 = w1 > w0 ? (w1 < (int64_t)P.warp_inc_off.size() ? (int64_t)P.warp_inc_off[w1]
+                                                                           : (int64_t)P.inc.size())
+                                   : 0;
+        ti.inc_off = (int32_t)i0;
+        ti.inc_words = (int32_t)(i1 - i0);
+        ti.pad0 = ti.pad1 = ti.pad2 = 0;
+        s->smem = std::max(s->smem, tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy));
+        max_ne = std::max<int64_t>(max_ne, ti.ne);
+        max_nact = std::max<int64_t>(max_nact, ti.nact);
+        max_incw = std::max<int64_t>(max_incw, ti.inc_words);
+        max_nh = std::max<int64_t>(max_nh, ti.nh);
+        max_slots = std::max<int64_t>(max_slots, ti.nm + ti.nh);
+        max_heavy = std::max<int64_t>(max_heavy, ti.nheavy);
     }
+    if (P.inc.size() > (size_t)INT32_MAX) return s->fail(TITAN_GB300_ELIMIT, "incidence table exceeds 2^31 words");
+    // shared-memory layout of the pipelined kernel (two stages)
+    {
+        auto al = [](int64_t x) { return (int32_t)((x + 15) & ~int64_t(15)); };
+        const int rec = tg::state_record_bytes(s->prec), ent = tg::entry_record_bytes(s->prec);
+        tg::PipeLayout &L = a.pipe;
+        L.rec = 0;
+        L.act = al(max_ne * ent);
+        L.inc = L.act + al(max_nact * ent);
+        L.st = L.inc + al(max_incw * 2);
+        L.stage = L.st + al(max_slots * rec);
+        L.idx = 2 * L.stage;
+        L.idx_bytes = al(((max_nh + 3) & ~int64_t(3)) * 4);
+        L.heavy = L.idx + 2 * L.idx_bytes;
+        L.mbar = al(L.heavy + 3 * max_heavy * (int64_t)rs);
+        L.total = L.mbar + 16;
+    }
+    s->use_pipe = s->kernel_req != 1 && a.pipe.total <= 227 * 1024;
+    if (s->kernel_req == 2 && !s->use_pipe)
+        return s->fail(TITAN_GB300_ELIMIT, "tiles too large for the pipelined kernel's two shared-memory stages");
+    if (s->use_pipe) {
+        CK(tg::step_pipe_prepare(s->prec, (size_t)a.pipe.total), "set shared memory");
+        int sms = 0, dev = 0, per_sm = 1;
+        CK(cudaGetDevice(&dev), "device");
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
+        per_sm = std::max(1, (227 * 1024) / a.pipe.total);
+        s->ctas = (int)std::min<int64_t>(P.ntiles, (int64_t)sms * per_sm);
+    } else {
+        if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
+        CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
+    }
+    a.ntiles = (int32_t)P.ntiles;
     if (P.ent_ends.size() > (size_t)INT32_MAX || P.halo.size() > (size_t)INT32_MAX)
         return s->fail(TITAN_GB300_ELIMIT, "more than 2^31 slab entries");
 #define DEVCOPY(dst, vec, what)                               \
@@ -411,6 +458,9 @@ int build_device(titan_gb300_sim *s) {
     if (!(a.tbuf = (double *)s->mem.get(2 * sizeof(double), e))) return s->cuda_fail(e, "alloc time");
     if (!(s->dprm = (tg::DevParams *)s->mem.get(sizeof(tg::DevParams), e))) return s->cuda_fail(e, "alloc params");
     a.prm = s->dprm;
+    if (!(s->d_err = (int *)s->mem.get(sizeof(int), e))) return s->cuda_fail(e, "alloc error flag");
+    CK(cudaMemset(s->d_err, 0, sizeof(int)), "clear error flag");
+    a.err = s->d_err;
     if (!(s->d_xfer = (double *)s->mem.get(9 * (size_t)s->n * 8, e))) return s->cuda_fail(e, "alloc staging");
     if (!(s->d_idx = (int64_t *)s->mem.get((size_t)s->n * 8, e))) return s->cuda_fail(e, "alloc staging");
     CK(cudaMallocHost(&s->h_xfer, 9 * (size_t)s->n * 8), "alloc pinned staging");
@@ -503,7 +553,7 @@ cudaGraphExec_t get_graph(titan_gb300_sim *s, int len, int parity, cudaError_t &
     if (e != cudaSuccess) return nullptr;
     int p = parity;
     for (int i = 0; i < len; i++) {
-        tg::launch_step(s->prec, s->args, (int)s->plan.ntiles, s->threads, s->smem, p, 0, s->stream);
+        s->launch(p, 0);
         p ^= 1;
     }
     e = cudaStreamEndCapture(s->stream, &g);
@@ -517,6 +567,18 @@ cudaGraphExec_t get_graph(titan_gb300_sim *s, int len, int parity, cudaError_t &
 }
 
 bool ensure_device(titan_gb300_sim *s) { return cudaSetDevice(s->device) == cudaSuccess; }
+
+// After a synchronisation: did a step kernel give up a bounded wait?
+int check_kernel_error(titan_gb300_sim *s) {
+    if (!s->d_err) return TITAN_GB300_OK;
+    int flag = 0;
+    CK(cudaMemcpy(&flag, s->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read error flag");
+    if (flag) {
+        cudaMemset(s->d_err, 0, sizeof(int));
+        return s->fail(TITAN_GB300_ETIMEOUT, "a step kernel's bounded wait for its shared-memory copies timed out");
+    }
+    return TITAN_GB300_OK;
+}
 
 }  // namespace
 
@@ -550,6 +612,23 @@ int titan_gb300_set_launch(titan_gb300_sim *s, int threads_per_cta) {
         return s->fail(TITAN_GB300_EINVAL, "threads per CTA must be 0 or a multiple of 32 in [64, 512]");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set the launch shape before start");
     s->threads_req = threads_per_cta;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (variant < 0 || variant > 2) return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0, 1 or 2");
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "choose the kernel before start");
+    s->kernel_req = variant;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
+    if (!s || !out) return TITAN_GB300_EINVAL;
+    out[0] = s->use_pipe ? 2 : 1;
+    out[1] = s->use_pipe ? s->ctas : s->plan.ntiles;
+    out[2] = s->threads;
+    out[3] = s->use_pipe ? s->args.pipe.total : (int64_t)s->smem;
     return TITAN_GB300_OK;
 }
 
@@ -588,6 +667,7 @@ int64_t titan_gb300_plan_table(const titan_gb300_sim *s, int table, void *out) {
         case TITAN_GB300_T_HEAVY_INC_OFF: return put(P.heavy_inc_off);
         case TITAN_GB300_T_HEAVY_INC: return put(P.heavy_inc);
         case TITAN_GB300_T_BODY_OF_TILE: return put(P.body_of_tile);
+        case TITAN_GB300_T_TILE_NH: return put(P.tile_nh);
         default: return -1;
     }
 }
@@ -786,7 +866,7 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
         s->parity ^= (len & 1);
         rem -= len;
     }
-    CK(tg::launch_step(s->prec, s->args, (int)s->plan.ntiles, s->threads, s->smem, s->parity, 1, s->stream),
+    CK(s->launch(s->parity, 1),
        "launch step");
     s->parity ^= 1;
     for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
@@ -798,7 +878,7 @@ int titan_gb300_synchronize(titan_gb300_sim *s) {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->stream) return TITAN_GB300_OK;
     CK(cudaStreamSynchronize(s->stream), "synchronize");
-    return TITAN_GB300_OK;
+    return check_kernel_error(s);
 }
 
 double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }
@@ -842,6 +922,7 @@ int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx
         CK(cudaMemcpyAsync(s->h_xfer, s->d_xfer, 9 * count * 8, cudaMemcpyDeviceToHost, s->stream), "download");
     }
     CK(cudaStreamSynchronize(s->stream), "download");
+    if (int rc = check_kernel_error(s)) return rc;
     if (pos) std::memcpy(pos, s->h_xfer, 3 * count * 8);
     if (vel) std::memcpy(vel, s->h_xfer + 3 * count, 3 * count * 8);
     if (acc) std::memcpy(acc, s->h_xfer + 6 * count, 3 * count * 8);

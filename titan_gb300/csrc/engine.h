@@ -29,7 +29,18 @@ constexpr int kMaxBalls = 16;
 struct TileInfo {
     int32_t mass_off, nm, halo_off, nh;
     int32_t ent_off, ne, nact, warp_off;
-    int32_t heavy_off, nheavy, body, pad;
+    int32_t heavy_off, nheavy, body, inc_off;  // inc_off: first u16 word of the tile's incidence block
+    int32_t inc_words, pad0, pad1, pad2;       // inc_words: length of that block (multiple of 128)
+};
+
+// Shared-memory layout of the pipelined step kernel (byte offsets).  Two
+// stages, each holding one tile's slab records, actuation records,
+// incidence block and state records (tile masses, then halo masses); two
+// halo-index buffers; heavy-mass sums; two mbarriers.
+struct PipeLayout {
+    int32_t rec, act, inc, st, stage;  // offsets inside a stage, stage size
+    int32_t idx, idx_bytes;            // first halo-index buffer, size of one
+    int32_t heavy, mbar, total;
 };
 
 struct DevParams {
@@ -72,6 +83,9 @@ struct StepArgs {
     const DevParams *prm;
     int64_t npad;
     int32_t slots, ecap, hcap;
+    int32_t ntiles;
+    int *err;                  // set by a kernel whose bounded wait gave up
+    PipeLayout pipe;
 };
 
 // Per-mass gather / scatter between caller order and tiled order.
@@ -109,6 +123,14 @@ size_t tile_smem_bytes(int precision, int slots, int entries, int heavy);
 cudaError_t step_prepare(int precision, size_t smem);
 cudaError_t launch_step(int precision, const StepArgs &a, int ntiles, int threads, size_t smem,
                         int parity, int write_acc, cudaStream_t s);
+// Pipelined persistent variant (step_tma.cu): grid of `ctas` CTAs walking the
+// tiles, TMA bulk copies of the next tile overlapping the current tile.
+cudaError_t step_pipe_prepare(int precision, size_t smem);
+cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int threads, int parity, int write_acc,
+                             cudaStream_t s);
+// bytes of one state record / one slab entry record for a precision
+int state_record_bytes(int precision);
+int entry_record_bytes(int precision);
 cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_scatter(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_diag(int precision, const DiagArgs &a, cudaStream_t s);

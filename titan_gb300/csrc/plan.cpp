@@ -196,6 +196,8 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     P.ent_spring.push_back(s);
                 }
             P.halo.insert(P.halo.end(), halo.begin(), halo.end());
+            while (P.halo.size() % 4) P.halo.push_back(halo.empty() ? (int32_t)lo : halo.back());
+            P.tile_nh.push_back((int32_t)nh);
             P.tile_nact.push_back((int32_t)ents_act.size());
 
             int nheavy = 0;

@@ -54,7 +54,8 @@ struct Plan {
     std::vector<int32_t> new2old, old2new;   // mass renumbering
     std::vector<int32_t> body_of_tile;
     std::vector<int64_t> tile_mass_off;      // ntiles+1 (new mass index)
-    std::vector<int64_t> tile_halo_off;      // ntiles+1
+    std::vector<int64_t> tile_halo_off;      // ntiles+1, multiples of 4 (16-byte aligned lists)
+    std::vector<int32_t> tile_nh;            // halo masses of each tile (lists are padded to 4)
     std::vector<int32_t> halo;               // new mass indices
     std::vector<int64_t> tile_ent_off;       // ntiles+1
     std::vector<int32_t> tile_nact;          // actuated entries lead each slab

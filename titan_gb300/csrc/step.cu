@@ -20,6 +20,8 @@
 #include <cstdint>
 
 #include "engine.h"
+#include "epilogue.cuh"
+#include "state.cuh"
 #include "step_math.cuh"
 
 namespace tg {
@@ -28,60 +30,6 @@ namespace {
 
 constexpr int kBatchB = 4;  // slab entries in flight per thread (phase B)
 constexpr int kBatchC = 4;  // 8-byte incidence words in flight per thread (phase C)
-
-// ------------------------------------------------------- state records ----
-template <int PREC>
-struct St {
-    float x[3], v[3], xl[3], vl[3];
-};
-template <>
-struct St<P_FP64> {
-    double x[3], v[3], xl[3], vl[3];
-};
-
-template <int PREC>
-__device__ __forceinline__ St<PREC> load_state(const void *buf, int64_t g) {
-    St<PREC> s;
-    if constexpr (PREC == P_FP64) {
-        const double2 *p = reinterpret_cast<const double2 *>(buf) + 3 * g;
-        double2 a0 = __ldg(p), a1 = __ldg(p + 1), a2 = __ldg(p + 2);
-        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a1.x;
-        s.v[0] = a1.y; s.v[1] = a2.x; s.v[2] = a2.y;
-    } else if constexpr (PREC == P_FP32C) {
-        const float4 *p = reinterpret_cast<const float4 *>(buf) + 3 * g;
-        float4 a0 = __ldg(p), a1 = __ldg(p + 1), a2 = __ldg(p + 2);
-        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a0.z;
-        s.v[0] = a0.w; s.v[1] = a1.x; s.v[2] = a1.y;
-        s.xl[0] = a1.z; s.xl[1] = a1.w; s.xl[2] = a2.x;
-        s.vl[0] = a2.y; s.vl[1] = a2.z; s.vl[2] = a2.w;
-    } else {
-        const float4 *p = reinterpret_cast<const float4 *>(buf) + 2 * g;
-        float4 a0 = __ldg(p);
-        float2 a1 = __ldg(reinterpret_cast<const float2 *>(p + 1));
-        s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a0.z;
-        s.v[0] = a0.w; s.v[1] = a1.x; s.v[2] = a1.y;
-    }
-    return s;
-}
-
-template <int PREC>
-__device__ __forceinline__ void store_state(void *buf, int64_t g, const St<PREC> &s) {
-    if constexpr (PREC == P_FP64) {
-        double2 *p = reinterpret_cast<double2 *>(buf) + 3 * g;
-        p[0] = make_double2(s.x[0], s.x[1]);
-        p[1] = make_double2(s.x[2], s.v[0]);
-        p[2] = make_double2(s.v[1], s.v[2]);
-    } else if constexpr (PREC == P_FP32C) {
-        float4 *p = reinterpret_cast<float4 *>(buf) + 3 * g;
-        p[0] = make_float4(s.x[0], s.x[1], s.x[2], s.v[0]);
-        p[1] = make_float4(s.v[1], s.v[2], s.xl[0], s.xl[1]);
-        p[2] = make_float4(s.xl[2], s.vl[0], s.vl[1], s.vl[2]);
-    } else {
-        float4 *p = reinterpret_cast<float4 *>(buf) + 2 * g;
-        p[0] = make_float4(s.x[0], s.x[1], s.x[2], s.v[0]);
-        p[1] = make_float4(s.v[1], s.v[2], 0.f, 0.f);
-    }
-}
 
 // ------------------------------------------------------------- kernel -----
 template <int PREC>
@@ -291,141 +239,18 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             s.x[c] = sx[c * S + i];
             s.v[c] = sv[c * S + i];
         }
-        if constexpr (PREC == P_FP64) {
-            double Fd[3] = {F0, F1, F2};
-            Fd[0] = Fd[0] + prm->g[0] * m;
-            Fd[1] = Fd[1] + prm->g[1] * m;
-            Fd[2] = Fd[2] + prm->g[2] * m;
-            if (fl & MF_EXT) {
-                const double *ext = reinterpret_cast<const double *>(a.ext);
-                Fd[0] = Fd[0] + ext[g];
-                Fd[1] = Fd[1] + ext[np + g];
-                Fd[2] = Fd[2] + ext[2 * np + g];
-            }
-            for (int j = 0; j < prm->nplanes; j++) {
-                const double *p = prm->plane[j];
-                plane_apply(p, p[3], p[4], p[5], s.x, s.v, Fd);
-            }
-            for (int j = 0; j < prm->nballs; j++) ball_apply(prm->ball[j], prm->ball[j][3], s.x, Fd);
-            if (fl & MF_BODYPLANE) {
-                const double *p = a.body_plane + 6 * (int64_t)ti.body;
-                plane_apply(p, p[3], p[4], p[5], s.x, s.v, Fd);
-            }
-            if (fl & MF_LOCAL) local_apply(a, g, s.x, s.v, Fd);
-            if (fl & MF_DRAG) {  // src/sim.cu:1134-1137
-                double vn = nrm3(s.v[0], s.v[1], s.v[2]);
-                if (vn != 0.0) {
-                    double c = (double)(-a.drag[g]) * (vn * vn);
-                    Fd[0] = Fd[0] + (s.v[0] * c) / vn;
-                    Fd[1] = Fd[1] + (s.v[1] * c) / vn;
-                    Fd[2] = Fd[2] + (s.v[2] * c) / vn;
-                }
-            }
-            const double dt = prm->dt;
-            double acc[3] = {Fd[0] / m, Fd[1] / m, Fd[2] / m};
+        if constexpr (PREC == P_FP32C) {
+            const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                s.v[c] = s.v[c] + acc[c] * dt;
-                s.x[c] = s.x[c] + s.v[c] * dt;
-            }
-            store_state<PREC>(out, g, s);
-            if (write_acc) {
-                double *ac = reinterpret_cast<double *>(a.acc);
-                ac[g] = acc[0];
-                ac[np + g] = acc[1];
-                ac[2 * np + g] = acc[2];
-            }
-        } else {
-            if constexpr (PREC == P_FP32C) {
-                const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
+            for (int c = 0; c < 3; c++) s.xl[c] = sxl[c * S + i];
+            s.vl[0] = a2.y;
+            s.vl[1] = a2.z;
+            s.vl[2] = a2.w;
+        } else if constexpr (PREC == P_FP32) {
 #pragma unroll
-                for (int c = 0; c < 3; c++) s.xl[c] = sxl[c * S + i];
-                s.vl[0] = a2.y;
-                s.vl[1] = a2.z;
-                s.vl[2] = a2.w;
-            } else {
-#pragma unroll
-                for (int c = 0; c < 3; c++) s.xl[c] = s.vl[c] = 0.f;
-            }
-            float Ff[3] = {fmaf(prm->gf[0], m, F0), fmaf(prm->gf[1], m, F1), fmaf(prm->gf[2], m, F2)};
-            if (fl & MF_EXT) {
-                const float *ext = reinterpret_cast<const float *>(a.ext);
-                Ff[0] += ext[g];
-                Ff[1] += ext[np + g];
-                Ff[2] += ext[2 * np + g];
-            }
-            float vv[3] = {s.v[0] + s.vl[0], s.v[1] + s.vl[1], s.v[2] + s.vl[2]};
-            for (int j = 0; j < prm->nplanes; j++) {
-                const float *p = prm->planef[j];
-                float disp = (dot3f(s.x, p) - p[3]) + dot3f(s.xl, p);
-                plane_applyf(p, disp, p[4], p[5], vv, Ff);
-            }
-            for (int j = 0; j < prm->nballs; j++) {
-                const float *b = prm->ballf[j];
-                float dd[3] = {(s.x[0] - b[0]) + s.xl[0], (s.x[1] - b[1]) + s.xl[1], (s.x[2] - b[2]) + s.xl[2]};
-                ball_applyf(dd, b[3], Ff);
-            }
-            if (fl & MF_BODYPLANE) {
-                const float *p = a.body_planef + 6 * (int64_t)ti.body;
-                float disp = (dot3f(s.x, p) - p[3]) + dot3f(s.xl, p);
-                plane_applyf(p, disp, p[4], p[5], vv, Ff);
-            }
-            if (fl & (MF_LOCAL | MF_DRAG)) {
-                // rare paths: evaluate in FP64 on the compensated values
-                double x[3], v[3], Fd[3], v0[3];
-                for (int c = 0; c < 3; c++) {
-                    x[c] = (double)s.x[c] + (double)s.xl[c];
-                    v0[c] = v[c] = (double)s.v[c] + (double)s.vl[c];
-                    Fd[c] = Ff[c];
-                }
-                if (fl & MF_LOCAL) local_apply(a, g, x, v, Fd);
-                if (fl & MF_DRAG) {
-                    double vn = nrm3(v[0], v[1], v[2]);
-                    if (vn != 0.0) {
-                        double c = (double)(-a.drag[g]) * (vn * vn);
-                        for (int k = 0; k < 3; k++) Fd[k] = Fd[k] + (v[k] * c) / vn;
-                    }
-                }
-                for (int c = 0; c < 3; c++) {
-                    Ff[c] = (float)Fd[c];
-                    if (v[c] != v0[c]) {  // a constraint projected the velocity
-                        s.v[c] = (float)v[c];
-                        s.vl[c] = (float)(v[c] - (double)s.v[c]);
-                    }
-                }
-            }
-            const float inv_m = __frcp_rn(m);
-            float acc[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                acc[c] = Ff[c] * inv_m;
-                if constexpr (PREC == P_FP32C) {
-                    // v += a dt with dt = dt_hi + dt_lo, compensated
-                    float p = acc[c] * prm->dt_hi;
-                    float pe = fmaf(acc[c], prm->dt_hi, -p) + acc[c] * prm->dt_lo;
-                    float sum, err;
-                    two_sum(s.v[c], p, sum, err);
-                    err += s.vl[c] + pe;
-                    fast_two_sum(sum, err, s.v[c], s.vl[c]);
-                    // x += v dt
-                    float q = s.v[c] * prm->dt_hi;
-                    float qe = fmaf(s.v[c], prm->dt_hi, -q) + fmaf(s.v[c], prm->dt_lo, s.vl[c] * prm->dt_hi);
-                    two_sum(s.x[c], q, sum, err);
-                    err += s.xl[c] + qe;
-                    fast_two_sum(sum, err, s.x[c], s.xl[c]);
-                } else {
-                    s.v[c] = s.v[c] + acc[c] * prm->dt_hi;
-                    s.x[c] = s.x[c] + s.v[c] * prm->dt_hi;
-                }
-            }
-            store_state<PREC>(out, g, s);
-            if (write_acc) {
-                float *ac = reinterpret_cast<float *>(a.acc);
-                ac[g] = acc[0];
-                ac[np + g] = acc[1];
-                ac[2 * np + g] = acc[2];
-            }
+            for (int c = 0; c < 3; c++) s.xl[c] = s.vl[c] = 0.f;
         }
+        integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, s, out, write_acc, np, prm);
     }
 }
 

@@ -1,0 +1,436 @@
+// step_tma.cu -- pipelined persistent form of the fused step (sm_103a).
+//
+// Same arithmetic, same per-mass summation order and same results as k_step
+// (step.cu) -- the tests check the two bit for bit -- but organised so that
+// HBM traffic overlaps computation:
+//   * a persistent grid (a few CTAs per SM) walks the tiles;
+//   * while a CTA computes tile k, the Tensor Memory Accelerator streams
+//     tile k+1's slab records, actuation records, incidence block and tile
+//     state records into the other shared-memory stage (cp.async.bulk with
+//     an mbarrier transaction count), and the CTA's threads fetch tile k+1's
+//     halo state records with 16-byte cp.async;
+//   * the halo index list of tile k+2 rides in tile k+1's bulk group, so the
+//     halo gathers can be issued a full tile ahead;
+//   * each entry's force overwrites its consumed record in shared memory, and
+//     the per-mass gather reads it back as one 16-byte vector.
+// Every mbarrier wait is bounded: on time-out the kernel sets *err, drains
+// its own copies (bounded) and returns; the host reports the error.
+#include <cstdint>
+
+#include "engine.h"
+#include "epilogue.cuh"
+#include "state.cuh"
+#include "step_math.cuh"
+
+namespace tg {
+
+namespace {
+
+constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 1-D bulk copy global -> shared, completion counted on bar (bytes % 16 == 0,
+// both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int PREC>
+struct Geo {
+    static constexpr int kRec = PREC == P_FP32 ? 32 : 48;  // state record bytes
+    static constexpr int kEnt = PREC == P_FP64 ? 32 : 16;  // slab / actuation record bytes
+};
+
+// Issues one tile's bulk copies into a stage; returns the byte count.
+__device__ __forceinline__ uint32_t issue_chunks(uint8_t *dst, const uint8_t *src, uint32_t bytes, uint64_t *bar) {
+    constexpr uint32_t kChunk = 32768;
+    for (uint32_t o = 0; o < bytes; o += kChunk) {
+        uint32_t b = bytes - o < kChunk ? bytes - o : kChunk;
+        bulk_g2s(dst + o, src + o, b, bar);
+    }
+    return bytes;
+}
+
+template <int PREC>
+__device__ __forceinline__ void issue_tile(const StepArgs &a, const TileInfo &ti, const void *in, uint8_t *stage,
+                                           const TileInfo *ti2, uint8_t *idxbuf, uint64_t *bar) {
+    using G = Geo<PREC>;
+    const PipeLayout &L = a.pipe;
+    uint32_t bytes = (uint32_t)ti.ne * G::kEnt + (uint32_t)ti.nact * G::kEnt + (uint32_t)ti.inc_words * 2 +
+                     (uint32_t)ti.nm * G::kRec;
+    uint32_t nh2 = ti2 ? (uint32_t)((ti2->nh + 3) & ~3) : 0u;
+    bytes += nh2 * 4;
+    mbar_expect_tx(bar, bytes);
+    const uint8_t *ent = reinterpret_cast<const uint8_t *>(a.ent) + (int64_t)ti.ent_off * G::kEnt;
+    const uint8_t *act = reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * G::kEnt;
+    issue_chunks(stage + L.rec, ent, (uint32_t)ti.ne * G::kEnt, bar);
+    issue_chunks(stage + L.act, act, (uint32_t)ti.nact * G::kEnt, bar);
+    issue_chunks(stage + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), (uint32_t)ti.inc_words * 2,
+                 bar);
+    issue_chunks(stage + L.st, reinterpret_cast<const uint8_t *>(in) + (int64_t)ti.mass_off * G::kRec,
+                 (uint32_t)ti.nm * G::kRec, bar);
+    if (nh2) issue_chunks(idxbuf, reinterpret_cast<const uint8_t *>(a.halo + ti2->halo_off), nh2 * 4, bar);
+}
+
+// Halo state records of tile ti into stage (after its tile masses).
+template <int PREC>
+__device__ __forceinline__ void issue_halo(const TileInfo &ti, const void *in, uint8_t *st, const int32_t *idx) {
+    using G = Geo<PREC>;
+    constexpr int kChunks = G::kRec / 16;
+    const int n = ti.nh * kChunks;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int h = q / kChunks, c = q - h * kChunks;
+        const uint8_t *src = reinterpret_cast<const uint8_t *>(in) + (int64_t)idx[h] * G::kRec + 16 * c;
+        cp_async16(st + (int64_t)(ti.nm + h) * G::kRec + 16 * c, src);
+    }
+}
+
+// Bounded wait on a stage's mbarrier; false (and *err set) on time-out.
+__device__ __forceinline__ bool wait_stage(const StepArgs &a, uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kWaitLimit; it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    atomicOr(a.err, 1);
+    return false;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int write_acc) {
+    using R = typename Real<PREC>::T;
+    using G = Geo<PREC>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    const PipeLayout &L = a.pipe;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.mbar);
+    R *sH = reinterpret_cast<R *>(smem + L.heavy);
+    const void *in = parity ? a.state1 : a.state0;
+    void *out = parity ? a.state0 : a.state1;
+    const int64_t np = a.npad;
+    const DevParams *prm = a.prm;
+    const double T = a.tbuf[parity];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = T + prm->dt;
+    const int ntiles = a.ntiles;
+    const int t0 = blockIdx.x;
+    if (t0 >= ntiles) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    // Pipeline invariant: at the start of iteration k (tile t0 + kG, stage
+    // k & 1), index buffer (k+1) & 1 holds the halo indices of tile
+    // t0 + (k+1)G.  Prologue: tile t0 (with its own halo indices in buffer 0)
+    // into stage 0, its halo gathers, and the indices of t0 + G into buffer 1.
+    uint32_t phase[2] = {0u, 0u};
+    const int G_ = gridDim.x;
+    const TileInfo first = a.tiles[t0];
+    if (threadIdx.x == 0) issue_tile<PREC>(a, first, in, smem, &first, smem + L.idx, &bars[0]);
+    // every wait outcome is made block-uniform before anyone acts on it
+    bool ok = !__syncthreads_or(!wait_stage(a, &bars[0], 0));
+    phase[0] ^= 1u;
+    if (ok) issue_halo<PREC>(first, in, smem + L.st, reinterpret_cast<const int32_t *>(smem + L.idx));
+    cp_async_commit();
+    if (t0 + G_ < ntiles) {
+        const TileInfo ti1 = a.tiles[t0 + G_];
+        int32_t *idx1 = reinterpret_cast<int32_t *>(smem + L.idx + L.idx_bytes);
+        for (int h = threadIdx.x; h < ti1.nh; h += blockDim.x) idx1[h] = __ldg(a.halo + ti1.halo_off + h);
+    }
+    __syncthreads();
+
+    int k = 0;
+    for (int t = t0; t < ntiles && ok; t += G_, k++) {
+        const int s = k & 1;
+        uint8_t *stage = smem + s * L.stage;
+        uint8_t *next_stage = smem + (s ^ 1) * L.stage;
+        const TileInfo ti = a.tiles[t];
+        const int tn = t + G_;
+        const bool has_next = tn < ntiles;
+        TileInfo tin{};
+        if (has_next) tin = a.tiles[tn];
+        // (a) bulk copies of tile t+G (and the halo indices of t+2G) into the other stage
+        if (threadIdx.x == 0 && has_next) {
+            const int tnn = tn + G_;
+            TileInfo tinn{};
+            if (tnn < ntiles) tinn = a.tiles[tnn];
+            fence_proxy_async();
+            issue_tile<PREC>(a, tin, in, next_stage, tnn < ntiles ? &tinn : nullptr,
+                             smem + L.idx + s * L.idx_bytes, &bars[s ^ 1]);
+        }
+        // per-mass scalars of this tile, needed only in phase C
+        const int i_own = threadIdx.x;
+        uint8_t fl = MF_FIXED;
+        uint32_t dg = 0, woff = 0;
+        R m = 1;
+        if (i_own < ti.nm) {
+            const int64_t g = (int64_t)ti.mass_off + i_own;
+            fl = __ldg(a.flags + g);
+            dg = __ldg(a.deg + g);
+            m = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+            woff = __ldg(a.warp_inc_off + ti.warp_off + (i_own >> 5)) - (uint32_t)ti.inc_off;
+        }
+        // (b) this tile's bulk data
+        if (k > 0) {
+            const bool timed_out = !wait_stage(a, &bars[s], phase[s]);
+            if (!timed_out) phase[s] ^= 1u;
+            if (__syncthreads_or(timed_out)) {
+                ok = false;
+                break;
+            }
+        }
+        // (c) halo gathers of the next tile (its indices are in buffer s^1)
+        if (has_next)
+            issue_halo<PREC>(tin, in, next_stage + L.st,
+                             reinterpret_cast<const int32_t *>(smem + L.idx + (s ^ 1) * L.idx_bytes));
+        cp_async_commit();
+        // (d) this tile's halo gathers (committed one group earlier)
+        cp_async_wait_1();
+        __syncthreads();
+
+        const uint8_t *st = stage + L.st;
+        uint8_t *recb = stage + L.rec;
+        const uint8_t *actb = stage + L.act;
+        const uint16_t *incs = reinterpret_cast<const uint16_t *>(stage + L.inc);
+
+        // ---- B: one force per slab entry, written over its record --------
+        if constexpr (PREC == P_FP64) {
+            for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
+                const double2 *rp = reinterpret_cast<const double2 *>(recb + (int64_t)e * 32);
+                const double2 r01 = rp[0], r23 = rp[1];
+                const uint32_t ends = (uint32_t)__double_as_longlong(r23.y);
+                const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
+                double scale = 1.0;
+                if (e < ti.nact) {
+                    const double2 *qp = reinterpret_cast<const double2 *>(actb + (int64_t)e * 32);
+                    const double2 q01 = qp[0], q23 = qp[1];
+                    double th = q01.x * T;
+                    th = th + q23.x;
+                    double sn = q01.y * sin(th);
+                    scale = ((ends >> 24) & 3) == 2 ? 1.0 - sn : 1.0 + sn;
+                }
+                const double2 *pa = reinterpret_cast<const double2 *>(st + (int64_t)sa * 48);
+                const double2 *pb = reinterpret_cast<const double2 *>(st + (int64_t)sb * 48);
+                const double2 a0 = pa[0], a1 = pa[1], b0 = pb[0], b1 = pb[1];
+                double d0 = b0.x - a0.x, d1 = b0.y - a0.y, d2 = b1.x - a1.x;
+                double nrm = nrm3(d0, d1, d2);
+                double u0 = d0 / nrm, u1 = d1 / nrm, u2 = d2 / nrm;
+                double fs = r01.x * (r01.y * scale - nrm);
+                double f0 = u0 * fs, f1 = u1 * fs, f2 = u2 * fs;
+                if (r23.x != 0.0) {
+                    const double2 a2 = pa[2], b2 = pb[2];
+                    double w0 = a1.y - b1.y, w1 = a2.x - b2.x, w2 = a2.y - b2.y;
+                    double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * r23.x;
+                    f0 = f0 + u0 * dd;
+                    f1 = f1 + u1 * dd;
+                    f2 = f2 + u2 * dd;
+                }
+                double2 *wp = reinterpret_cast<double2 *>(recb + (int64_t)e * 32);
+                wp[0] = make_double2(f0, f1);
+                wp[1] = make_double2(f2, 0.0);
+            }
+        } else {
+            const float Thi = (float)T;
+            const float Tlo = (float)(T - (double)Thi);
+            for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
+                float4 *rp = reinterpret_cast<float4 *>(recb) + e;
+                const float4 r = *rp;
+                const uint32_t ends = __float_as_uint(r.x);
+                const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
+                float rs = r.z;
+                if (e < ti.nact) {
+                    const float4 q = reinterpret_cast<const float4 *>(actb)[e];
+                    float th = fmaf(q.x, Thi, fmaf(q.x, Tlo, q.z));
+                    float sn = q.y * sinf(th);
+                    rs = r.z * (((ends >> 24) & 3) == 2 ? 1.0f - sn : 1.0f + sn);
+                }
+                constexpr int kV = G::kRec / 16;  // float4 per state record
+                const float4 *pa = reinterpret_cast<const float4 *>(st) + sa * kV;
+                const float4 *pb = reinterpret_cast<const float4 *>(st) + sb * kV;
+                const float4 a0 = pa[0], a1 = pa[1], b0 = pb[0], b1 = pb[1];
+                float d0 = b0.x - a0.x, d1 = b0.y - a0.y, d2 = b0.z - a0.z;
+                if constexpr (PREC == P_FP32C) {
+                    const float4 a2 = pa[2], b2 = pb[2];
+                    d0 += b1.z - a1.z;
+                    d1 += b1.w - a1.w;
+                    d2 += b2.x - a2.x;
+                }
+                float nrm = nrm3f(d0, d1, d2);
+                float inv = __frcp_rn(nrm);
+                float u0 = d0 * inv, u1 = d1 * inv, u2 = d2 * inv;
+                float f = r.y * (rs - nrm);
+                if (r.w != 0.f) {
+                    float w0 = a0.w - b0.w, w1 = a1.x - b1.x, w2 = a1.y - b1.y;
+                    f = fmaf(fmaf(w2, u2, fmaf(w1, u1, w0 * u0)), r.w, f);
+                }
+                *rp = make_float4(u0 * f, u1 * f, u2 * f, 0.f);
+            }
+        }
+        __syncthreads();
+
+        // ---- C0: heavy masses (warp-cooperative, fixed order) --------------
+        if (ti.nheavy > 0) {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            for (int h = warp; h < ti.nheavy; h += nw) {
+                const int64_t gh = (int64_t)ti.heavy_off + h;
+                const uint32_t q0 = a.heavy_inc_off[gh], q1 = a.heavy_inc_off[gh + 1];
+                R p0 = 0, p1 = 0, p2 = 0;
+                for (uint32_t q = q0 + lane; q < q1; q += 32) {
+                    const uint32_t code = a.heavy_inc[q];
+                    const int idx = code & 0x7fff;
+                    const R *f = reinterpret_cast<const R *>(recb + (int64_t)idx * G::kEnt);
+                    if (code & 0x8000) {
+                        p0 = p0 + (-f[0]);
+                        p1 = p1 + (-f[1]);
+                        p2 = p2 + (-f[2]);
+                    } else {
+                        p0 = p0 + f[0];
+                        p1 = p1 + f[1];
+                        p2 = p2 + f[2];
+                    }
+                }
+#pragma unroll
+                for (int off = 16; off >= 1; off >>= 1) {
+                    p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, off);
+                    p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, off);
+                    p2 = p2 + __shfl_xor_sync(0xffffffffu, p2, off);
+                }
+                if (lane == 0) {
+                    sH[h] = p0;
+                    sH[ti.nheavy + h] = p1;
+                    sH[2 * ti.nheavy + h] = p2;
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- C: per-mass gather, constraints, integration ------------------
+        for (int i = threadIdx.x; i < ti.nm; i += blockDim.x) {
+            const int64_t g = (int64_t)ti.mass_off + i;
+            uint8_t fli = fl;
+            uint32_t d = dg, wo = woff;
+            R mi = m;
+            if (i != i_own) {  // more masses than threads
+                fli = __ldg(a.flags + g);
+                d = __ldg(a.deg + g);
+                mi = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+                wo = __ldg(a.warp_inc_off + ti.warp_off + (i >> 5)) - (uint32_t)ti.inc_off;
+            }
+            if (fli & MF_FIXED) continue;
+            R F0 = 0, F1 = 0, F2 = 0;
+            if (d == 255) {
+                int h = 0;
+                while (h < ti.nheavy && a.heavy_local[ti.heavy_off + h] != i) h++;
+                F0 = F0 + sH[h];
+                F1 = F1 + sH[ti.nheavy + h];
+                F2 = F2 + sH[2 * ti.nheavy + h];
+            } else {
+                const uint2 *ip = reinterpret_cast<const uint2 *>(incs + wo) + (i & 31);
+                const uint32_t nw = (d + 3) >> 2;
+                for (uint32_t w = 0; w < nw; w++) {
+                    const uint2 cw = ip[32 * w];
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        const uint32_t j = 4 * w + h;
+                        if (j < d) {
+                            const uint32_t word = h < 2 ? cw.x : cw.y;
+                            const uint32_t code = (word >> (16 * (h & 1))) & 0xffffu;
+                            const int idx = code & 0x7fff;
+                            if constexpr (PREC == P_FP64) {
+                                const double2 *f = reinterpret_cast<const double2 *>(recb + (int64_t)idx * 32);
+                                const double2 f01 = f[0], f2v = f[1];
+                                if (code & 0x8000) {
+                                    F0 = F0 + (-f01.x);
+                                    F1 = F1 + (-f01.y);
+                                    F2 = F2 + (-f2v.x);
+                                } else {
+                                    F0 = F0 + f01.x;
+                                    F1 = F1 + f01.y;
+                                    F2 = F2 + f2v.x;
+                                }
+                            } else {
+                                const float4 f = reinterpret_cast<const float4 *>(recb)[idx];
+                                if (code & 0x8000) {
+                                    F0 = F0 + (-f.x);
+                                    F1 = F1 + (-f.y);
+                                    F2 = F2 + (-f.z);
+                                } else {
+                                    F0 = F0 + f.x;
+                                    F1 = F1 + f.y;
+                                    F2 = F2 + f.z;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            St<PREC> sv = load_state_smem<PREC>(st, i);
+            integrate<PREC>(a, ti, g, fli, mi, F0, F1, F2, sv, out, write_acc, np, prm);
+        }
+        __syncthreads();  // the stage and the index buffer are free again
+    }
+    if (!ok) {
+        // drain this CTA's own copies before returning (bounded)
+        cp_async_wait_all();
+        for (int s = 0; s < 2; s++) {
+            uint32_t it = 0;
+            while (it++ < kWaitLimit && !mbar_try_wait(&bars[s], phase[s])) {
+            }
+        }
+    } else {
+        cp_async_wait_all();
+    }
+}
+
+}  // namespace
+
+int state_record_bytes(int precision) { return precision == P_FP32 ? 32 : 48; }
+int entry_record_bytes(int precision) { return precision == P_FP64 ? 32 : 16; }
+
+cudaError_t step_pipe_prepare(int precision, size_t smem) {
+    const void *f = precision == P_FP64   ? (const void *)k_step_pipe<P_FP64>
+                    : precision == P_FP32 ? (const void *)k_step_pipe<P_FP32>
+                                          : (const void *)k_step_pipe<P_FP32C>;
+    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int threads, int parity, int write_acc,
+                             cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    const size_t smem = (size_t)a.pipe.total;
+    switch (precision) {
+        case P_FP64: k_step_pipe<P_FP64><<<ctas, threads, smem, s>>>(a, parity, write_acc); break;
+        case P_FP32: k_step_pipe<P_FP32><<<ctas, threads, smem, s>>>(a, parity, write_acc); break;
+        default: k_step_pipe<P_FP32C><<<ctas, threads, smem, s>>>(a, parity, write_acc); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace tg

@@ -153,7 +153,7 @@ def config3(nbodies=4096, seed=3, side_range=(3, 12), spacing=0.1, pitch=2.0):
     return sc
 
 
-def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0):
+def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0):
     """Upload a scene into a Sim handle (and start it)."""
     sim.set_time_step(sc["dt"])
     sim.set_global_acc(sc["g"])
@@ -174,10 +174,12 @@ def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0):
                 sim.set_body_plane(b, n, off, fk, fs)
     if threads:
         sim.set_launch(threads)
+    if kernel:
+        sim.set_kernel(kernel)
     if start:
         sim.start(tile_masses)
     return sim
 
 
-def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0) -> Sim:
-    return load(Sim(precision, device), sc, True, tile_masses, threads)
+def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0, kernel=0) -> Sim:
+    return load(Sim(precision, device), sc, True, tile_masses, threads, kernel)
