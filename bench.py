@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--threads", type=int, default=0)
+    p.add_argument("--kernel", type=int, default=0, help="0 auto, 1 per-tile, 2 pipelined")
     return p.parse_args()
 
 
@@ -185,8 +186,9 @@ def run_ours(a, rank, world, local):
         barrier()
         return e0.elapsed_time(e1)
 
-    sim = wl.make_sim(sc, prec, a.tile, device=local, threads=a.threads)
+    sim = wl.make_sim(sc, prec, a.tile, device=local, threads=a.threads, kernel=a.kernel)
     info = sim.plan_info()
+    kinfo = sim.kernel_info()
     sim.step(a.warmup)
     sim.synchronize()
     with ClockSampler(local) as clk:
@@ -249,7 +251,8 @@ def run_ours(a, rank, world, local):
                                "plane + ball, dt=1e-4", "masses": nm, "springs": ns,
                    "precision": a.precision, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "per-step working set larger than L2 (no flush)", "tiles": info["tiles"],
-                   "threads_per_cta": info["threads"], "smem_bytes": info["smem_bytes"]},
+                   "kernel": kinfo["kernel"], "ctas": kinfo["ctas"], "threads_per_cta": kinfo["threads"],
+                   "smem_bytes": kinfo["smem_bytes"]},
         "mass_updates_per_s": nm * a.steps * world / (ms_max / 1e3),
         "hbm_algorithmic_gbs": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -141,6 +141,7 @@ private:
     std::vector<Mass *> graveyard;
     std::vector<Spring *> spring_graveyard;
     titan_gb300_sim *handle = nullptr;
+    long steps_base = 0;  // steps run by handles replaced in topology rebuilds
     int precision_ = 0;
     bool dirty = false;  // topology changed since the device scene was built
     std::vector<Mass *> built_masses;

@@ -166,7 +166,7 @@ def test_kernel_forms_bitwise_identical(precision, scene, tile):
 
 def test_pipelined_kernel_with_few_ctas_per_tile_list():
     """Tiles walked by a persistent grid: more tiles than CTAs, odd counts."""
-    sc = wl.lattice_scene((0, 0, 1.0), (2, 2, 2), 23, 21, 19, k=3e3, damping=0.1)
+    sc = wl.lattice_scene((0, 0, 1.0), (2, 2, 2), 41, 39, 37, k=3e3, damping=0.1)
     sc["planes"].append(((0.0, 0.0, 1.0), 0.0, 0.5, 0.5))
     _, a = gpu_run(sc, 300, tg.FP64, tile=32, kernel=1)
     s, b = gpu_run(sc, 300, tg.FP64, tile=32, kernel=2)

@@ -27,10 +27,12 @@ BUILD = PKG / "_build"
 ORACLE = ROOT / "oracle"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+# --fmad=false: every kernel rounds each product and sum separately, as the
+# CPU oracle does (FP64 parity), and the two step-kernel forms stay
+# bit-identical in every precision; explicit fmaf() calls are unaffected.
+NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
                "-I", str(ROOT / "include"), "-I", str(CSRC)]
-# the FP64 step must round every product and sum separately (parity with the oracle)
-NVCC_KERNEL_EXTRA = {"step.cu": ["--fmad=false"]}
+NVCC_KERNEL_EXTRA: dict[str, list[str]] = {}
 CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 
@@ -70,6 +72,13 @@ def build_library(verbose: bool = False) -> Path:
     jobs = []
     objs = []
     hdrs = _headers()
+    # a change of compiler flags invalidates every object
+    sig = BUILD / "flags.txt"
+    flags = " ".join(ARCH + NVCC_COMMON + CXX_COMMON)
+    if not sig.exists() or sig.read_text() != flags:
+        for o in BUILD.glob("*.o"):
+            o.unlink()
+        sig.write_text(flags)
     for f in LIB_CU:
         src, obj = CSRC / f, BUILD / (f + ".o")
         objs.append(obj)

@@ -400,12 +400,16 @@ int build_device(titan_gb300_sim *s) {
         L.idx_bytes = al(((max_nh + 3) & ~int64_t(3)) * 4);
         L.heavy = L.idx + 2 * L.idx_bytes;
         L.mbar = al(L.heavy + 3 * max_heavy * (int64_t)rs);
-        L.total = L.mbar + 16;
+        L.tinfo = L.mbar + 16;
+        L.total = L.tinfo + tg::kPipeTileCache * (int32_t)sizeof(tg::TileInfo);
     }
     s->use_pipe = s->kernel_req != 1 && a.pipe.total <= 227 * 1024;
     if (s->kernel_req == 2 && !s->use_pipe)
         return s->fail(TITAN_GB300_ELIMIT, "tiles too large for the pipelined kernel's two shared-memory stages");
     if (s->use_pipe) {
+        // a persistent CTA computes every slab entry of its tiles: give it
+        // more warps than a tile has masses
+        if (s->threads_req == 0) s->threads = std::max(256, s->threads);
         CK(tg::step_pipe_prepare(s->prec, (size_t)a.pipe.total), "set shared memory");
         int sms = 0, dev = 0, per_sm = 1;
         CK(cudaGetDevice(&dev), "device");

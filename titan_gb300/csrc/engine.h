@@ -40,8 +40,9 @@ struct TileInfo {
 struct PipeLayout {
     int32_t rec, act, inc, st, stage;  // offsets inside a stage, stage size
     int32_t idx, idx_bytes;            // first halo-index buffer, size of one
-    int32_t heavy, mbar, total;
+    int32_t heavy, mbar, tinfo, total; // tinfo: cached TileInfo of the CTA's first kPipeTileCache tiles
 };
+constexpr int kPipeTileCache = 64;
 
 struct DevParams {
     double dt;

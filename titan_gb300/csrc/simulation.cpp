@@ -353,6 +353,7 @@ void Simulation::buildDevice(bool keep_device_state) {
         for (int64_t i = 0; i < on; i++) old_index[built_masses[i]] = i;
     }
     double Tnow = T.load();
+    if (handle) steps_base += (long)titan_gb300_steps(handle);
     if (handle) titan_gb300_destroy(handle);
     handle = nullptr;
     titan_gb300_sim *h = nullptr;
@@ -586,7 +587,7 @@ void Simulation::step(long n) {
     T = titan_gb300_time(handle);
 }
 
-long Simulation::steps() { return handle ? (long)titan_gb300_steps(handle) : 0; }
+long Simulation::steps() { return steps_base + (handle ? (long)titan_gb300_steps(handle) : 0); }
 
 void Simulation::diagnostics(double g_mag, double energy[4], double momentum[6]) {
     if (!STARTED || ENDED) throw std::runtime_error("diagnostics needs a started simulation");

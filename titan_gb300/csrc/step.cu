@@ -28,8 +28,9 @@ namespace tg {
 
 namespace {
 
-constexpr int kBatchB = 4;  // slab entries in flight per thread (phase B)
-constexpr int kBatchC = 4;  // 8-byte incidence words in flight per thread (phase C)
+constexpr int kBatchB = 4;     // slab entries in flight per thread (phase B)
+constexpr int kBatchC = 4;     // 8-byte incidence words in flight per thread (phase C)
+constexpr int kPrefetchW = 8;  // incidence words (32 codes) fetched before phase B
 
 // ------------------------------------------------------------- kernel -----
 template <int PREC>
@@ -50,16 +51,56 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
     const double T = a.tbuf[parity];
     if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = T + prm->dt;
 
-    // ---- A: stage tile + halo -------------------------------------------
-    for (int i = threadIdx.x; i < S; i += blockDim.x) {
-        int64_t g = i < ti.nm ? (int64_t)ti.mass_off + i : (int64_t)__ldg(a.halo + ti.halo_off + i - ti.nm);
-        St<PREC> s = load_state<PREC>(in, g);
+    // per-mass inputs of phase C for this thread's own mass, issued now so
+    // that their latency hides behind phases A and B
+    const int i_own = threadIdx.x;
+    uint8_t fl_own = MF_FIXED;
+    uint32_t d_own = 0, woff_own = 0;
+    R m_own = 1;
+    float vl_own[3] = {0.f, 0.f, 0.f};
+    uint2 cw_own[kPrefetchW];
+    if (i_own < ti.nm) {
+        const int64_t g = (int64_t)ti.mass_off + i_own;
+        fl_own = __ldg(a.flags + g);
+        d_own = __ldg(a.deg + g);
+        m_own = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+        woff_own = __ldg(a.warp_inc_off + ti.warp_off + (i_own >> 5));
+        if constexpr (PREC == P_FP32C) {
+            const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
+            vl_own[0] = a2.y;
+            vl_own[1] = a2.z;
+            vl_own[2] = a2.w;
+        }
+    }
+
+    // ---- A: stage tile + halo (two records in flight per thread) ---------
+    for (int i0 = threadIdx.x; i0 < S; i0 += 2 * blockDim.x) {
+        const int i1 = i0 + blockDim.x;
+        const int64_t g0 = i0 < ti.nm ? (int64_t)ti.mass_off + i0 : (int64_t)__ldg(a.halo + ti.halo_off + i0 - ti.nm);
+        int64_t g1 = g0;
+        if (i1 < S) g1 = i1 < ti.nm ? (int64_t)ti.mass_off + i1 : (int64_t)__ldg(a.halo + ti.halo_off + i1 - ti.nm);
+        const St<PREC> s0 = load_state<PREC>(in, g0);
+        St<PREC> s1 = s0;
+        if (i1 < S) s1 = load_state<PREC>(in, g1);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            sx[c * S + i] = s.x[c];
-            sv[c * S + i] = s.v[c];
-            if constexpr (PREC == P_FP32C) sxl[c * S + i] = s.xl[c];
+            sx[c * S + i0] = s0.x[c];
+            sv[c * S + i0] = s0.v[c];
+            if constexpr (PREC == P_FP32C) sxl[c * S + i0] = s0.xl[c];
+            if (i1 < S) {
+                sx[c * S + i1] = s1.x[c];
+                sv[c * S + i1] = s1.v[c];
+                if constexpr (PREC == P_FP32C) sxl[c * S + i1] = s1.xl[c];
+            }
         }
+    }
+    // the first incidence words of this thread's mass (needs woff_own, d_own)
+    if (i_own < ti.nm && d_own != 255) {
+        const uint2 *ip = reinterpret_cast<const uint2 *>(a.inc + woff_own) + (i_own & 31);
+        const uint32_t nw = (d_own + 3) >> 2;
+#pragma unroll
+        for (int w = 0; w < kPrefetchW; w++)
+            if ((uint32_t)w < nw) cw_own[w] = __ldg(ip + 32 * w);
     }
     __syncthreads();
 
@@ -190,11 +231,33 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
     // ---- C: per-mass gather, constraints, integration ----------------------
     for (int i = threadIdx.x; i < ti.nm; i += blockDim.x) {
         const int64_t g = (int64_t)ti.mass_off + i;
-        const uint8_t fl = __ldg(a.flags + g);
+        const bool own = i == i_own;
+        const uint8_t fl = own ? fl_own : __ldg(a.flags + g);
         if (fl & MF_FIXED) continue;  // src/sim.cu:1100
-        const uint32_t d = __ldg(a.deg + g);
-        const R m = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+        const uint32_t d = own ? d_own : __ldg(a.deg + g);
+        const R m = own ? m_own : __ldg(reinterpret_cast<const R *>(a.mass) + g);
         R F0 = 0, F1 = 0, F2 = 0;
+        // codes 4w..4w+3 of one incidence word, in ascending order
+        auto add_word = [&](const uint2 cw, uint32_t w) {
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const uint32_t j = 4 * w + h;
+                if (j < d) {
+                    const uint32_t word = h < 2 ? cw.x : cw.y;
+                    const uint32_t code = (word >> (16 * (h & 1))) & 0xffffu;
+                    const int idx = code & 0x7fff;
+                    if (code & 0x8000) {
+                        F0 = F0 + (-sF[idx]);
+                        F1 = F1 + (-sF[E + idx]);
+                        F2 = F2 + (-sF[2 * E + idx]);
+                    } else {
+                        F0 = F0 + sF[idx];
+                        F1 = F1 + sF[E + idx];
+                        F2 = F2 + sF[2 * E + idx];
+                    }
+                }
+            }
+        };
         if (d == 255) {
             int h = 0;
             while (h < ti.nheavy && a.heavy_local[ti.heavy_off + h] != i) h++;
@@ -202,35 +265,24 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             F1 = F1 + sH[ti.nheavy + h];
             F2 = F2 + sH[2 * ti.nheavy + h];
         } else if (d > 0) {
-            const uint2 *ip =
-                reinterpret_cast<const uint2 *>(a.inc + a.warp_inc_off[ti.warp_off + (i >> 5)]) + (i & 31);
+            const uint32_t woff = own ? woff_own : __ldg(a.warp_inc_off + ti.warp_off + (i >> 5));
+            const uint2 *ip = reinterpret_cast<const uint2 *>(a.inc + woff) + (i & 31);
             const uint32_t nw = (d + 3) >> 2;
-            for (uint32_t w0 = 0; w0 < nw; w0 += kBatchC) {
+            uint32_t w0 = 0;
+            if (own) {
+#pragma unroll
+                for (int w = 0; w < kPrefetchW; w++)
+                    if ((uint32_t)w < nw) add_word(cw_own[w], w);
+                w0 = kPrefetchW;
+            }
+            for (; w0 < nw; w0 += kBatchC) {
                 uint2 cw[kBatchC];
 #pragma unroll
                 for (int k = 0; k < kBatchC; k++)
                     if (w0 + k < nw) cw[k] = __ldg(ip + 32 * (w0 + k));
 #pragma unroll
-                for (int k = 0; k < kBatchC; k++) {
-#pragma unroll
-                    for (int h = 0; h < 4; h++) {
-                        const uint32_t j = 4 * (w0 + k) + h;
-                        if (j < d) {
-                            const uint32_t word = h < 2 ? cw[k].x : cw[k].y;
-                            const uint32_t code = (word >> (16 * (h & 1))) & 0xffffu;
-                            const int idx = code & 0x7fff;
-                            if (code & 0x8000) {
-                                F0 = F0 + (-sF[idx]);
-                                F1 = F1 + (-sF[E + idx]);
-                                F2 = F2 + (-sF[2 * E + idx]);
-                            } else {
-                                F0 = F0 + sF[idx];
-                                F1 = F1 + sF[E + idx];
-                                F2 = F2 + sF[2 * E + idx];
-                            }
-                        }
-                    }
-                }
+                for (int k = 0; k < kBatchC; k++)
+                    if (w0 + k < nw) add_word(cw[k], w0 + k);
             }
         }
         St<PREC> s;
@@ -240,12 +292,18 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             s.v[c] = sv[c * S + i];
         }
         if constexpr (PREC == P_FP32C) {
-            const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
 #pragma unroll
             for (int c = 0; c < 3; c++) s.xl[c] = sxl[c * S + i];
-            s.vl[0] = a2.y;
-            s.vl[1] = a2.z;
-            s.vl[2] = a2.w;
+            if (own) {
+                s.vl[0] = vl_own[0];
+                s.vl[1] = vl_own[1];
+                s.vl[2] = vl_own[2];
+            } else {
+                const float4 a2 = __ldg(reinterpret_cast<const float4 *>(in) + 3 * g + 2);
+                s.vl[0] = a2.y;
+                s.vl[1] = a2.z;
+                s.vl[2] = a2.w;
+            }
         } else if constexpr (PREC == P_FP32) {
 #pragma unroll
             for (int c = 0; c < 3; c++) s.xl[c] = s.vl[c] = 0.f;

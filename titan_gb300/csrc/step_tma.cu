@@ -144,6 +144,21 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
         mbar_init(&bars[1], 1);
         fence_mbar_init();
     }
+    // this CTA's tile descriptors (tiles t0, t0+G, ...), cached so that no
+    // iteration waits on a global load before issuing its copies
+    TileInfo *tcache = reinterpret_cast<TileInfo *>(smem + L.tinfo);
+    {
+        const int words = (int)(sizeof(TileInfo) / 4);
+        for (int q = threadIdx.x; q < kPipeTileCache * words; q += blockDim.x) {
+            const int k = q / words, w = q - k * words;
+            const int t = blockIdx.x + k * (int)gridDim.x;
+            if (t < ntiles)
+                reinterpret_cast<int32_t *>(tcache + k)[w] = __ldg(reinterpret_cast<const int32_t *>(a.tiles + t) + w);
+        }
+    }
+    auto tile = [&](int k) -> TileInfo {
+        return k < kPipeTileCache ? tcache[k] : a.tiles[blockIdx.x + k * (int)gridDim.x];
+    };
     __syncthreads();
 
     // Pipeline invariant: at the start of iteration k (tile t0 + kG, stage
@@ -152,7 +167,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
     // into stage 0, its halo gathers, and the indices of t0 + G into buffer 1.
     uint32_t phase[2] = {0u, 0u};
     const int G_ = gridDim.x;
-    const TileInfo first = a.tiles[t0];
+    const TileInfo first = tile(0);
     if (threadIdx.x == 0) issue_tile<PREC>(a, first, in, smem, &first, smem + L.idx, &bars[0]);
     // every wait outcome is made block-uniform before anyone acts on it
     bool ok = !__syncthreads_or(!wait_stage(a, &bars[0], 0));
@@ -160,7 +175,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
     if (ok) issue_halo<PREC>(first, in, smem + L.st, reinterpret_cast<const int32_t *>(smem + L.idx));
     cp_async_commit();
     if (t0 + G_ < ntiles) {
-        const TileInfo ti1 = a.tiles[t0 + G_];
+        const TileInfo ti1 = tile(1);
         int32_t *idx1 = reinterpret_cast<int32_t *>(smem + L.idx + L.idx_bytes);
         for (int h = threadIdx.x; h < ti1.nh; h += blockDim.x) idx1[h] = __ldg(a.halo + ti1.halo_off + h);
     }
@@ -171,16 +186,16 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
         const int s = k & 1;
         uint8_t *stage = smem + s * L.stage;
         uint8_t *next_stage = smem + (s ^ 1) * L.stage;
-        const TileInfo ti = a.tiles[t];
+        const TileInfo ti = tile(k);
         const int tn = t + G_;
         const bool has_next = tn < ntiles;
         TileInfo tin{};
-        if (has_next) tin = a.tiles[tn];
+        if (has_next) tin = tile(k + 1);
         // (a) bulk copies of tile t+G (and the halo indices of t+2G) into the other stage
         if (threadIdx.x == 0 && has_next) {
             const int tnn = tn + G_;
             TileInfo tinn{};
-            if (tnn < ntiles) tinn = a.tiles[tnn];
+            if (tnn < ntiles) tinn = tile(k + 2);
             fence_proxy_async();
             issue_tile<PREC>(a, tin, in, next_stage, tnn < ntiles ? &tinn : nullptr,
                              smem + L.idx + s * L.idx_bytes, &bars[s ^ 1]);
