@@ -208,6 +208,27 @@ int titan_gb300_set_spring_params(titan_gb300_sim *sim, int64_t count, const int
 int titan_gb300_diagnostics(titan_gb300_sim *sim, double g_mag, double energy[4],
                             double momentum[6]);
 
+/* The same FP64 energy and momentum as titan_gb300_diagnostics, for callers
+ * that must not allocate device memory when they ask (memory reserved once at
+ * start-up, a host framework whose caching allocator owns the device, work
+ * issued while a stream is being captured).  No counterpart in the reference.
+ * It allocates nothing: inputs and the output are the caller's device
+ * buffers -- pos, vel (3n doubles, xyz-interleaved), m (n), left/right (ns
+ * int32, -1 = skipped), k, rest (ns) -- and out receives 9 doubles (spring
+ * PE, kinetic, gravity PE = g_mag z m, linear momentum xyz, angular momentum
+ * xyz), queued on stream (a cudaStream_t, NULL = default stream).  Scratch
+ * is a 288 KiB array compiled into the library, held on every GPU that loads
+ * it until the process exits.  n and ns may be at most 4096 * 256 * 64
+ * (67,108,864); larger sizes return TITAN_GB300_ELIMIT without launching.
+ * The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * Calls share the array: two calls that overlap on the GPU race and must be
+ * ordered by the caller. */
+int titan_gb300_diagnostics_noalloc(const double *pos, const double *vel, const double *m, int64_t n,
+                                    const int32_t *left, const int32_t *right, const double *k,
+                                    const double *rest, int64_t ns, double g_mag, double *out,
+                                    void *stream);
+
 /* CUDA stream (cudaStream_t) the handle queues work on. */
 void *titan_gb300_stream(titan_gb300_sim *sim);
 
