@@ -291,9 +291,13 @@ int upload_entries(titan_gb300_sim *s) {
             ent[4 * e + 1] = (float)s->k[j];
             ent[4 * e + 2] = (float)s->rest[j];
             ent[4 * e + 3] = (float)s->damping[j];
-            act[4 * e] = (float)sp_omega(j);
-            act[4 * e + 1] = (float)sp_amp(j);
-            act[4 * e + 2] = (float)sp_phase(j);
+            // rest' = rest (1 + a sin(2 pi (nu T + phi))): nu = omega / 2 pi,
+            // phi = phase / 2 pi, a = -amp for contract-then-expand (type 2)
+            const double two_pi = 6.283185307179586476925286766559;
+            const int ty = s->type.empty() ? 0 : s->type[j];
+            act[4 * e] = (float)(sp_omega(j) / two_pi);
+            act[4 * e + 1] = (float)(ty == 2 ? -sp_amp(j) : sp_amp(j));
+            act[4 * e + 2] = (float)(sp_phase(j) / two_pi);
         }
         CK(cudaMemcpy(const_cast<void *>(a.ent), ent.data(), ent.size() * 4, cudaMemcpyHostToDevice), "upload ent");
         CK(cudaMemcpy(const_cast<void *>(a.act), act.data(), act.size() * 4, cudaMemcpyHostToDevice), "upload act");
@@ -328,8 +332,8 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.slot_cap = 4095;
     in.entry_cap = 32767;
     in.smem_budget = 220 * 1024;
-    in.slot_bytes = (s->prec == P_FP32C ? 9 : 6) * rs;
-    in.entry_bytes = 3 * rs;
+    in.slot_bytes = tg::state_record_bytes(s->prec);
+    in.entry_bytes = tg::entry_record_bytes(s->prec);
     in.heavy_bytes = 3 * rs;
     return in;
 }

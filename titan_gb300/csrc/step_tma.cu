@@ -21,6 +21,7 @@
 #include "epilogue.cuh"
 #include "state.cuh"
 #include "step_math.cuh"
+#include "tile_phases.cuh"
 
 namespace tg {
 
@@ -134,8 +135,8 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
     void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
-    const double T = a.tbuf[parity];
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = T + prm->dt;
+    const StepTime tm = step_time(a.tbuf[parity]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + prm->dt;
     const int ntiles = a.ntiles;
     const int t0 = blockIdx.x;
     if (t0 >= ntiles) return;
@@ -236,113 +237,18 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
         const uint16_t *incs = reinterpret_cast<const uint16_t *>(stage + L.inc);
 
         // ---- B: one force per slab entry, written over its record --------
-        if constexpr (PREC == P_FP64) {
-            for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
-                const double2 *rp = reinterpret_cast<const double2 *>(recb + (int64_t)e * 32);
-                const double2 r01 = rp[0], r23 = rp[1];
-                const uint32_t ends = (uint32_t)__double_as_longlong(r23.y);
-                const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
-                double scale = 1.0;
-                if (e < ti.nact) {
-                    const double2 *qp = reinterpret_cast<const double2 *>(actb + (int64_t)e * 32);
-                    const double2 q01 = qp[0], q23 = qp[1];
-                    double th = q01.x * T;
-                    th = th + q23.x;
-                    double sn = q01.y * sin(th);
-                    scale = ((ends >> 24) & 3) == 2 ? 1.0 - sn : 1.0 + sn;
-                }
-                const double2 *pa = reinterpret_cast<const double2 *>(st + (int64_t)sa * 48);
-                const double2 *pb = reinterpret_cast<const double2 *>(st + (int64_t)sb * 48);
-                const double2 a0 = pa[0], a1 = pa[1], b0 = pb[0], b1 = pb[1];
-                double d0 = b0.x - a0.x, d1 = b0.y - a0.y, d2 = b1.x - a1.x;
-                double nrm = nrm3(d0, d1, d2);
-                double u0 = d0 / nrm, u1 = d1 / nrm, u2 = d2 / nrm;
-                double fs = r01.x * (r01.y * scale - nrm);
-                double f0 = u0 * fs, f1 = u1 * fs, f2 = u2 * fs;
-                if (r23.x != 0.0) {
-                    const double2 a2 = pa[2], b2 = pb[2];
-                    double w0 = a1.y - b1.y, w1 = a2.x - b2.x, w2 = a2.y - b2.y;
-                    double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * r23.x;
-                    f0 = f0 + u0 * dd;
-                    f1 = f1 + u1 * dd;
-                    f2 = f2 + u2 * dd;
-                }
-                double2 *wp = reinterpret_cast<double2 *>(recb + (int64_t)e * 32);
-                wp[0] = make_double2(f0, f1);
-                wp[1] = make_double2(f2, 0.0);
-            }
-        } else {
-            const float Thi = (float)T;
-            const float Tlo = (float)(T - (double)Thi);
-            for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
-                float4 *rp = reinterpret_cast<float4 *>(recb) + e;
-                const float4 r = *rp;
-                const uint32_t ends = __float_as_uint(r.x);
-                const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
-                float rs = r.z;
-                if (e < ti.nact) {
-                    const float4 q = reinterpret_cast<const float4 *>(actb)[e];
-                    float th = fmaf(q.x, Thi, fmaf(q.x, Tlo, q.z));
-                    float sn = q.y * sinf(th);
-                    rs = r.z * (((ends >> 24) & 3) == 2 ? 1.0f - sn : 1.0f + sn);
-                }
-                constexpr int kV = G::kRec / 16;  // float4 per state record
-                const float4 *pa = reinterpret_cast<const float4 *>(st) + sa * kV;
-                const float4 *pb = reinterpret_cast<const float4 *>(st) + sb * kV;
-                const float4 a0 = pa[0], a1 = pa[1], b0 = pb[0], b1 = pb[1];
-                float d0 = b0.x - a0.x, d1 = b0.y - a0.y, d2 = b0.z - a0.z;
-                if constexpr (PREC == P_FP32C) {
-                    const float4 a2 = pa[2], b2 = pb[2];
-                    d0 += b1.z - a1.z;
-                    d1 += b1.w - a1.w;
-                    d2 += b2.x - a2.x;
-                }
-                float nrm = nrm3f(d0, d1, d2);
-                float inv = __frcp_rn(nrm);
-                float u0 = d0 * inv, u1 = d1 * inv, u2 = d2 * inv;
-                float f = r.y * (rs - nrm);
-                if (r.w != 0.f) {
-                    float w0 = a0.w - b0.w, w1 = a1.x - b1.x, w2 = a1.y - b1.y;
-                    f = fmaf(fmaf(w2, u2, fmaf(w1, u1, w0 * u0)), r.w, f);
-                }
-                *rp = make_float4(u0 * f, u1 * f, u2 * f, 0.f);
-            }
+        for (int e = threadIdx.x; e < ti.ne; e += blockDim.x) {
+            uint8_t *slot = recb + (int64_t)e * G::kEnt;
+            const bool actuated = e < ti.nact;
+            const Rec16<PREC> r = load_rec<PREC>(slot);
+            const Rec16<PREC> q = actuated ? load_rec<PREC>(actb + (int64_t)e * G::kEnt) : r;
+            entry_force<PREC>(r, actuated, q, st, tm, slot);
         }
         __syncthreads();
 
         // ---- C0: heavy masses (warp-cooperative, fixed order) --------------
         if (ti.nheavy > 0) {
-            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-            for (int h = warp; h < ti.nheavy; h += nw) {
-                const int64_t gh = (int64_t)ti.heavy_off + h;
-                const uint32_t q0 = a.heavy_inc_off[gh], q1 = a.heavy_inc_off[gh + 1];
-                R p0 = 0, p1 = 0, p2 = 0;
-                for (uint32_t q = q0 + lane; q < q1; q += 32) {
-                    const uint32_t code = a.heavy_inc[q];
-                    const int idx = code & 0x7fff;
-                    const R *f = reinterpret_cast<const R *>(recb + (int64_t)idx * G::kEnt);
-                    if (code & 0x8000) {
-                        p0 = p0 + (-f[0]);
-                        p1 = p1 + (-f[1]);
-                        p2 = p2 + (-f[2]);
-                    } else {
-                        p0 = p0 + f[0];
-                        p1 = p1 + f[1];
-                        p2 = p2 + f[2];
-                    }
-                }
-#pragma unroll
-                for (int off = 16; off >= 1; off >>= 1) {
-                    p0 = p0 + __shfl_xor_sync(0xffffffffu, p0, off);
-                    p1 = p1 + __shfl_xor_sync(0xffffffffu, p1, off);
-                    p2 = p2 + __shfl_xor_sync(0xffffffffu, p2, off);
-                }
-                if (lane == 0) {
-                    sH[h] = p0;
-                    sH[ti.nheavy + h] = p1;
-                    sH[2 * ti.nheavy + h] = p2;
-                }
-            }
+            heavy_sums<PREC>(a, ti, recb, sH);
             __syncthreads();
         }
 
@@ -369,42 +275,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
             } else {
                 const uint2 *ip = reinterpret_cast<const uint2 *>(incs + wo) + (i & 31);
                 const uint32_t nw = (d + 3) >> 2;
-                for (uint32_t w = 0; w < nw; w++) {
-                    const uint2 cw = ip[32 * w];
-#pragma unroll
-                    for (int h = 0; h < 4; h++) {
-                        const uint32_t j = 4 * w + h;
-                        if (j < d) {
-                            const uint32_t word = h < 2 ? cw.x : cw.y;
-                            const uint32_t code = (word >> (16 * (h & 1))) & 0xffffu;
-                            const int idx = code & 0x7fff;
-                            if constexpr (PREC == P_FP64) {
-                                const double2 *f = reinterpret_cast<const double2 *>(recb + (int64_t)idx * 32);
-                                const double2 f01 = f[0], f2v = f[1];
-                                if (code & 0x8000) {
-                                    F0 = F0 + (-f01.x);
-                                    F1 = F1 + (-f01.y);
-                                    F2 = F2 + (-f2v.x);
-                                } else {
-                                    F0 = F0 + f01.x;
-                                    F1 = F1 + f01.y;
-                                    F2 = F2 + f2v.x;
-                                }
-                            } else {
-                                const float4 f = reinterpret_cast<const float4 *>(recb)[idx];
-                                if (code & 0x8000) {
-                                    F0 = F0 + (-f.x);
-                                    F1 = F1 + (-f.y);
-                                    F2 = F2 + (-f.z);
-                                } else {
-                                    F0 = F0 + f.x;
-                                    F1 = F1 + f.y;
-                                    F2 = F2 + f.z;
-                                }
-                            }
-                        }
-                    }
-                }
+                for (uint32_t w = 0; w < nw; w++) gather_word<PREC>(recb, ip[32 * w], w, d, F0, F1, F2);
             }
             St<PREC> sv = load_state_smem<PREC>(st, i);
             integrate<PREC>(a, ti, g, fli, mi, F0, F1, F2, sv, out, write_acc, np, prm);
