@@ -143,10 +143,10 @@ int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
  * tile size itself is start()'s argument.  Used by the autotuner. */
 int titan_gb300_set_launch(titan_gb300_sim *sim, int threads_per_cta);
 
-/* Step kernel form: 0 = automatic (the pipelined persistent kernel whenever
- * two of the scene's tiles fit in shared memory, else the per-tile kernel),
- * 1 = per-tile kernel (one CTA per tile), 2 = pipelined kernel (fails at
- * start() when the tiles are too large).  Both forms give bit-identical
+/* Step kernel form: 0 = automatic (currently the per-tile kernel, the faster
+ * form measured on GB300), 1 = per-tile kernel (one CTA per tile), 2 =
+ * pipelined persistent kernel (TMA-staged tiles; fails at start() when two
+ * tiles do not fit in shared memory).  Both forms give bit-identical
  * results.  Set before start(). */
 int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
 

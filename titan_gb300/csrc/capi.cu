@@ -324,7 +324,7 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 64 : 128);
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : 256);
     in.heavy_threshold = 96;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)
@@ -407,7 +407,9 @@ int build_device(titan_gb300_sim *s) {
         L.tinfo = L.mbar + 16;
         L.total = L.tinfo + tg::kPipeTileCache * (int32_t)sizeof(tg::TileInfo);
     }
-    s->use_pipe = s->kernel_req != 1 && a.pipe.total <= 227 * 1024;
+    // automatic choice: the per-tile form (measured faster on GB300 for the
+    // lattice workloads, see the kernel-form sweep in profiles/)
+    s->use_pipe = s->kernel_req == 2 && a.pipe.total <= 227 * 1024;
     if (s->kernel_req == 2 && !s->use_pipe)
         return s->fail(TITAN_GB300_ELIMIT, "tiles too large for the pipelined kernel's two shared-memory stages");
     if (s->use_pipe) {
