@@ -154,6 +154,28 @@ int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
  * out[2] threads per CTA, out[3] dynamic shared memory per CTA (bytes). */
 int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
 
+/* Batched bodies (no reference counterpart: the reference runs one scene
+ * per process, src/sim.cu:1503-1617).  With resident bins on, every body
+ * (set_bodies) that fits one CTA -- no spring to another body, every free
+ * mass of degree <= 254, 2 state records per mass in shared memory -- is
+ * packed with others into a bin of at most bin_masses masses, and one
+ * persistent launch per step() call runs all nsteps steps of every bin with
+ * the state held in shared memory; the remaining bodies take the per-step
+ * kernels.  Results are bit-identical to the per-step kernels.
+ *   mode 0: off (default: on GB300 the per-step kernels measured faster
+ *   for batches whose spring records exceed shared memory); 1 on.  bin_masses: bin capacity, rounded up to a multiple of 32 (0:
+ *   max(1024, largest fitting body)); bodies above it are not resident.
+ *   threads_per_cta
+ *   0: derived from the bin size; else a multiple of 32 in [64, 512].
+ * Set before start(). */
+int titan_gb300_set_resident(titan_gb300_sim *sim, int mode, int bin_masses, int threads_per_cta);
+
+/* After start(): out[0] 1 if resident bins are in use, out[1] bins,
+ * out[2] resident bodies, out[3] resident masses, out[4] bin capacity
+ * (masses), out[5] threads per CTA, out[6] CTAs per launch, out[7] dynamic
+ * shared memory per CTA (bytes). */
+int titan_gb300_resident_info(const titan_gb300_sim *sim, int64_t out[8]);
+
 /* One iteration of the reference's execute() loop body (src/sim.cu:1569-1590)
  * nsteps times: spring forces + mass update fused into one kernel per step,
  * replayed from cached CUDA graphs.  Asynchronous. */
@@ -265,6 +287,17 @@ int64_t titan_gb300_plan_table(const titan_gb300_sim *sim, int table, void *out)
 #define TITAN_GB300_T_HEAVY_INC 15     /* uint16                                 */
 #define TITAN_GB300_T_BODY_OF_TILE 16  /* int32                                  */
 #define TITAN_GB300_T_TILE_NH 17       /* int32: halo masses of each tile (HALO lists are padded to 4) */
+/* resident bins (set_resident): */
+#define TITAN_GB300_T_RES_BIN_MASS_OFF 18 /* int64: nbins+1, into RES_MASS       */
+#define TITAN_GB300_T_RES_BIN_WARP_OFF 19 /* int64: nbins+1, into RES_WARP_REC_OFF */
+#define TITAN_GB300_T_RES_MASS 20      /* int32: tiled index of each resident mass */
+#define TITAN_GB300_T_RES_BODY 21      /* int32: its body                        */
+#define TITAN_GB300_T_RES_DEG 22       /* uint8: its degree (0 if fixed)         */
+#define TITAN_GB300_T_RES_ACT_MASK 23  /* uint64: bit j = record j is actuated   */
+#define TITAN_GB300_T_RES_WARP_REC_OFF 24 /* uint32: first record of each bin warp */
+#define TITAN_GB300_T_RES_WORDS 25     /* uint32: other (bin-local) | 0x8000 if right end | type << 16 */
+#define TITAN_GB300_T_RES_REC_SPRING 26 /* int64: spring of each record, -1 = padding */
+#define TITAN_GB300_T_RES_RESIDENT 27  /* uint8: per body, 1 if resident         */
 
 /* Lattice builder of createLattice (src/sim.cu:1923-1944, src/object.cu:232-293):
  * fills pos (3*nx*ny*nz) and, when non-NULL, left/right/rest of the

@@ -193,3 +193,119 @@ def test_plan_rejects_hub_beyond_slab():
           "k": np.ones(n - 1), "rest": np.ones(n - 1), "planes": [], "balls": [], "g": np.zeros(3), "dt": 1e-4}
     with pytest.raises(tg.TitanError, match="ELIMIT"):
         plan_tables(sc, 64)
+
+
+# ------------------------------------------------- resident bin plan -------
+RT = {"bin_mass_off": (18, np.int64), "bin_warp_off": (19, np.int64), "mass": (20, np.int32),
+      "body": (21, np.int32), "deg": (22, np.uint8), "act_mask": (23, np.uint64), "warp_rec_off": (24, np.uint32),
+      "words": (25, np.uint32), "rec_spring": (26, np.int64), "resident": (27, np.uint8)}
+
+
+def resident_tables(sc, resident, precision=tg.FP32C):
+    s = tg.Sim(precision)
+    wl.load(s, sc, start=False, resident=resident)
+    s._check(s._L.titan_gb300_plan_host(s._h, 64), "plan_host")
+    out = {}
+    for name, (idx, dt) in list(RT.items()) + [("new2old", (0, np.int32))]:
+        n = s._L.titan_gb300_plan_table(s._h, idx, None)
+        a = np.zeros(max(n, 0), dt)
+        s._L.titan_gb300_plan_table(s._h, idx, a.ctypes.data_as(ctypes.c_void_p))
+        out[name] = a
+    s.close()
+    return out
+
+
+def validate_resident(sc, R, cap):
+    n = sc["pos"].shape[0]
+    left, right, typ = sc["left"], sc["right"], sc["type"]
+    fixed = np.zeros(n, bool) if sc.get("fixed") is None else np.asarray(sc["fixed"], bool)
+    bp = sc["body_ptr"]
+    nb = bp.size - 1
+    body_of = np.repeat(np.arange(nb), np.diff(bp))
+    old2new = np.empty(n, np.int64)
+    old2new[R["new2old"]] = np.arange(n)
+    valid = (left >= 0) & (right >= 0) & (left < n) & (right < n)
+    cross = np.zeros(nb, bool)
+    for s in np.flatnonzero(valid):
+        if body_of[left[s]] != body_of[right[s]]:
+            cross[body_of[left[s]]] = cross[body_of[right[s]]] = True
+    # expected incidence (ascending springs) of every free mass, creation order
+    inc = [[] for _ in range(n)]
+    for s in np.flatnonzero(valid):
+        if not fixed[right[s]]:
+            inc[right[s]].append((s, left[s], 1))
+        if not fixed[left[s]]:
+            inc[left[s]].append((s, right[s], 0))
+    for b in range(nb):
+        nm = bp[b + 1] - bp[b]
+        fits = nm <= cap and not cross[b] and max(len(inc[i]) for i in range(bp[b], bp[b + 1])) <= 254
+        assert bool(R["resident"][b]) == fits, b
+    nbins = R["bin_mass_off"].size - 1
+    seen = set()
+    for k in range(nbins):
+        m0, m1 = R["bin_mass_off"][k], R["bin_mass_off"][k + 1]
+        assert 0 < m1 - m0 <= cap
+        tiled = R["mass"][m0:m1]
+        old = R["new2old"][tiled]
+        bodies = set(body_of[old].tolist())
+        assert all(R["resident"][b] for b in bodies)
+        # whole bodies, each once
+        assert sum(bp[b + 1] - bp[b] for b in bodies) == m1 - m0
+        assert not (bodies & seen)
+        seen |= bodies
+        assert (R["body"][m0:m1] == body_of[old]).all()
+        local = {int(g): q for q, g in enumerate(tiled)}
+        w0 = R["bin_warp_off"][k]
+        assert R["bin_warp_off"][k + 1] - w0 == (m1 - m0 + 31) // 32
+        for q in range(m1 - m0):
+            i = old[q]
+            d = R["deg"][m0 + q]
+            assert d == len(inc[i])
+            mask = 0
+            for j, (s, other, is_right) in enumerate(inc[i]):
+                r = R["warp_rec_off"][w0 + q // 32] + 32 * j + q % 32
+                assert R["rec_spring"][r] == s
+                w = int(R["words"][r])
+                assert w & 0x7FFF == local[int(old2new[other])]
+                assert bool(w & 0x8000) == bool(is_right)
+                assert (w >> 16) & 3 == typ[s] & 3
+                if j < 64 and typ[s] >= 2:
+                    mask |= 1 << j
+            assert int(R["act_mask"][m0 + q]) == mask
+    assert seen == set(np.flatnonzero(R["resident"]).tolist())
+    # bins are ordered by decreasing work
+    work = [R["deg"][R["bin_mass_off"][k]:R["bin_mass_off"][k + 1]].sum() + np.diff(R["bin_mass_off"])[k]
+            for k in range(nbins)]
+    assert all(work[k] >= work[k + 1] for k in range(nbins - 1))
+
+
+def test_resident_plan_bins():
+    sc = wl.config3(nbodies=30, seed=5, side_range=(3, 7))
+    rng = np.random.default_rng(1)
+    sc["fixed"] = (rng.random(sc["pos"].shape[0]) < 0.05).astype(np.uint8)
+    validate_resident(sc, resident_tables(sc, (1, 512, 0)), 512)
+
+
+def test_resident_plan_excludes_large_and_coupled_bodies():
+    sc = wl.config3(nbodies=16, seed=6, side_range=(3, 8))
+    bp = sc["body_ptr"]
+    # a spring between bodies 0 and 1 keeps both on the per-step kernels
+    for key, val in (("left", bp[0]), ("right", bp[1]), ("k", 1e3), ("rest", 1.0), ("damping", 0.0), ("type", 0),
+                     ("omega", 0.0), ("amp", 0.2), ("phase", 0.0)):
+        sc[key] = np.concatenate([sc[key], [val]]).astype(sc[key].dtype)
+    R = resident_tables(sc, (1, 128, 64))  # 64 threads: bins of at most 4 * 64 masses
+    cap = 128
+    validate_resident(sc, R, cap)
+    assert not R["resident"][0] and not R["resident"][1]
+    sizes = np.diff(bp)
+    assert (R["resident"][sizes > cap] == 0).all()
+
+
+def test_set_resident_validates():
+    s = tg.Sim(tg.FP32C)
+    for args in ((2, 0, 0), (-1, 0, 0), (1, -5, 0), (1, 0, 100), (1, 0, 1024)):
+        with pytest.raises(tg.TitanError, match="EINVAL"):
+            s.set_resident(*args)
+    s.set_resident(1, 512, 128)
+    s.set_resident(0)
+    s.close()

@@ -19,8 +19,8 @@ from titan_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 
 
-def gpu_run(sc, nsteps, precision=tg.FP64, tile=0, chunks=None, kernel=0, threads=0):
-    s = wl.make_sim(sc, precision, tile, kernel=kernel, threads=threads)
+def gpu_run(sc, nsteps, precision=tg.FP64, tile=0, chunks=None, kernel=0, threads=0, resident=None):
+    s = wl.make_sim(sc, precision, tile, kernel=kernel, threads=threads, resident=resident)
     if chunks:
         for c in chunks:
             s.step(c)
@@ -114,7 +114,7 @@ def test_bodies_with_own_planes_bitwise():
     sc = wl.config3(nbodies=24, seed=9, side_range=(3, 7))
     for key in ("type",):
         sc[key][:] = 0  # passive: bitwise bar
-    _, st = gpu_run(sc, 3000, tile=128)
+    _, st = gpu_run(sc, 3000, tile=128, resident=(0, 0, 0))
     o = oracle_run(sc, 3000)
     assert_bitwise(st, o)
 
@@ -157,8 +157,8 @@ def test_kernel_forms_bitwise_identical(precision, scene, tile):
     """The pipelined persistent kernel (TMA-staged tiles) and the per-tile
     kernel give identical bits in every precision."""
     sc = kernel_scenes()[scene]
-    s1, a = gpu_run(sc, 700, precision, tile=tile, kernel=1)
-    s2, b = gpu_run(sc, 700, precision, tile=tile, kernel=2)
+    s1, a = gpu_run(sc, 700, precision, tile=tile, kernel=1, resident=(0, 0, 0))
+    s2, b = gpu_run(sc, 700, precision, tile=tile, kernel=2, resident=(0, 0, 0))
     assert s1.kernel_info()["kernel"] == "per-tile" and s2.kernel_info()["kernel"] == "pipelined"
     for k in ("pos", "vel", "acc", "T"):
         assert np.array_equal(a[k], b[k]), k

@@ -63,6 +63,8 @@ _SIGS = {
     "titan_gb300_set_launch": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_kernel": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_kernel_info": (ctypes.c_int, [_P, _I64]),
+    "titan_gb300_set_resident": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "titan_gb300_resident_info": (ctypes.c_int, [_P, _I64]),
     "titan_gb300_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "titan_gb300_synchronize": (ctypes.c_int, [_P]),
     "titan_gb300_time": (ctypes.c_double, [_P]),
@@ -259,6 +261,17 @@ class Sim:
         self._check(self._L.titan_gb300_kernel_info(self._h, _ptr(out, ctypes.c_int64)), "kernel_info")
         return {"kernel": "pipelined" if out[0] == 2 else "per-tile", "ctas": int(out[1]), "threads": int(out[2]),
                 "smem_bytes": int(out[3])}
+
+    def set_resident(self, mode: int = 1, bin_masses: int = 0, threads: int = 0):
+        """Resident bins for batched bodies: mode 0 off (default), 1 on; bin
+        capacity in masses and CTA size (0: default)."""
+        self._check(self._L.titan_gb300_set_resident(self._h, mode, bin_masses, threads), "set_resident")
+
+    def resident_info(self) -> dict:
+        out = np.zeros(8, np.int64)
+        self._check(self._L.titan_gb300_resident_info(self._h, _ptr(out, ctypes.c_int64)), "resident_info")
+        keys = ("active", "bins", "bodies", "masses", "cap", "threads", "ctas", "smem_bytes")
+        return {k: int(v) for k, v in zip(keys, out)}
 
     def start(self, tile_masses: int = 0):
         self._check(self._L.titan_gb300_start(self._h, tile_masses), "start")

@@ -110,10 +110,19 @@ struct titan_gb300_sim {
     bool use_pipe = false;
     int ctas = 0;         // persistent grid of the pipelined kernel
     int *d_err = nullptr;
+    // body-resident batched launch
+    int res_mode = 0;     // 0 off, 1 on
+    int res_bin_req = 0;  // bin capacity in masses (0: default)
+    int res_threads_req = 0;
+    tg::ResPlan rplan;
+    tg::ResArgs rargs{};
+    bool use_res = false;
+    int res_threads = 0, res_ctas = 0;
 
     cudaError_t launch(int parity, int write_acc) {
+        if (args.ntiles == 0) return cudaSuccess;
         if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
-        return tg::launch_step(prec, args, (int)plan.ntiles, threads, smem, parity, write_acc, stream);
+        return tg::launch_step(prec, args, (int)args.ntiles, threads, smem, parity, write_acc, stream);
     }
 
     int fail(int code, const std::string &msg) {
@@ -258,35 +267,39 @@ int upload_mass_attrs(titan_gb300_sim *s) {
     return TITAN_GB300_OK;
 }
 
-// Slab entry records and actuation parameters from the host spring arrays.
-int upload_entries(titan_gb300_sim *s) {
-    const tg::Plan &P = s->plan;
-    const size_t E = P.ent_ends.size();
-    auto &a = s->args;
+// Spring records (slab-entry layout: FP64 k, rest, damping, word; FP32
+// word, k, rest, damping) and actuation records for the springs spring[e]
+// with entry words word[e] (spring -1: a zero padding record), uploaded to
+// rec / act.
+int upload_records(titan_gb300_sim *s, const std::vector<int64_t> &spring, const std::vector<uint32_t> &word,
+                   void *rec, void *act) {
+    const size_t E = spring.size();
     if (E == 0) return TITAN_GB300_OK;
     auto sp_amp = [&](int64_t j) { return s->amp.empty() ? 0.2 : s->amp[j]; };
     auto sp_phase = [&](int64_t j) { return s->phase.empty() ? 0.0 : s->phase[j]; };
     auto sp_omega = [&](int64_t j) { return s->omega.empty() ? 0.0 : s->omega[j]; };
     if (s->prec == P_FP64) {
-        std::vector<double> ent(4 * E), act(4 * E, 0.0);
+        std::vector<double> ent(4 * E, 0.0), ac(4 * E, 0.0);
         for (size_t e = 0; e < E; e++) {
-            int64_t j = P.ent_spring[e];
+            int64_t j = spring[e];
+            if (j < 0) continue;
             ent[4 * e] = s->k[j];
             ent[4 * e + 1] = s->rest[j];
             ent[4 * e + 2] = s->damping[j];
-            uint64_t bits = P.ent_ends[e];
+            uint64_t bits = word[e];
             std::memcpy(&ent[4 * e + 3], &bits, 8);
-            act[4 * e] = sp_omega(j);
-            act[4 * e + 1] = sp_amp(j);
-            act[4 * e + 2] = sp_phase(j);
+            ac[4 * e] = sp_omega(j);
+            ac[4 * e + 1] = sp_amp(j);
+            ac[4 * e + 2] = sp_phase(j);
         }
-        CK(cudaMemcpy(const_cast<void *>(a.ent), ent.data(), ent.size() * 8, cudaMemcpyHostToDevice), "upload ent");
-        CK(cudaMemcpy(const_cast<void *>(a.act), act.data(), act.size() * 8, cudaMemcpyHostToDevice), "upload act");
+        CK(cudaMemcpy(rec, ent.data(), ent.size() * 8, cudaMemcpyHostToDevice), "upload records");
+        CK(cudaMemcpy(act, ac.data(), ac.size() * 8, cudaMemcpyHostToDevice), "upload actuation");
     } else {
-        std::vector<float> ent(4 * E), act(4 * E, 0.f);
+        std::vector<float> ent(4 * E, 0.f), ac(4 * E, 0.f);
         for (size_t e = 0; e < E; e++) {
-            int64_t j = P.ent_spring[e];
-            uint32_t bits = P.ent_ends[e];
+            int64_t j = spring[e];
+            if (j < 0) continue;
+            uint32_t bits = word[e];
             std::memcpy(&ent[4 * e], &bits, 4);
             ent[4 * e + 1] = (float)s->k[j];
             ent[4 * e + 2] = (float)s->rest[j];
@@ -295,14 +308,27 @@ int upload_entries(titan_gb300_sim *s) {
             // phi = phase / 2 pi, a = -amp for contract-then-expand (type 2)
             const double two_pi = 6.283185307179586476925286766559;
             const int ty = s->type.empty() ? 0 : s->type[j];
-            act[4 * e] = (float)(sp_omega(j) / two_pi);
-            act[4 * e + 1] = (float)(ty == 2 ? -sp_amp(j) : sp_amp(j));
-            act[4 * e + 2] = (float)(sp_phase(j) / two_pi);
+            ac[4 * e] = (float)(sp_omega(j) / two_pi);
+            ac[4 * e + 1] = (float)(ty == 2 ? -sp_amp(j) : sp_amp(j));
+            ac[4 * e + 2] = (float)(sp_phase(j) / two_pi);
         }
-        CK(cudaMemcpy(const_cast<void *>(a.ent), ent.data(), ent.size() * 4, cudaMemcpyHostToDevice), "upload ent");
-        CK(cudaMemcpy(const_cast<void *>(a.act), act.data(), act.size() * 4, cudaMemcpyHostToDevice), "upload act");
+        CK(cudaMemcpy(rec, ent.data(), ent.size() * 4, cudaMemcpyHostToDevice), "upload records");
+        CK(cudaMemcpy(act, ac.data(), ac.size() * 4, cudaMemcpyHostToDevice), "upload actuation");
     }
     return TITAN_GB300_OK;
+}
+
+// Slab entry records and actuation parameters from the host spring arrays,
+// and the resident bins' records.
+int upload_entries(titan_gb300_sim *s) {
+    const tg::Plan &P = s->plan;
+    auto &a = s->args;
+    int rc = upload_records(s, P.ent_spring, P.ent_ends, const_cast<void *>(a.ent), const_cast<void *>(a.act));
+    if (rc) return rc;
+    if (s->use_res)
+        rc = upload_records(s, s->rplan.rec_spring, s->rplan.words, const_cast<void *>(s->rargs.rec),
+                            const_cast<void *>(s->rargs.act));
+    return rc;
 }
 
 template <typename T>
@@ -336,6 +362,26 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.entry_bytes = tg::entry_record_bytes(s->prec);
     in.heavy_bytes = 3 * rs;
     return in;
+}
+
+// Bin capacity of the resident plan (0: no resident bins): two state
+// records per mass must fit one CTA's shared memory, with at most
+// kResMaxMpt masses per thread.
+int resident_cap(const titan_gb300_sim *s) {
+    const int64_t nb = s->body_ptr.empty() ? 1 : (int64_t)s->body_ptr.size() - 1;
+    const bool want = s->res_mode == 1;
+    if (!want) return 0;
+    const int rec = tg::state_record_bytes(s->prec);
+    int lim = (int)(((227 * 1024 - 1024) / (2 * rec)) & ~31);
+    lim = std::min(lim, tg::kResMaxMpt * (s->res_threads_req > 0 ? s->res_threads_req : 512));
+    int64_t big = 0;
+    for (int64_t b = 0; b < nb; b++) {
+        const int64_t m = s->body_ptr.empty() ? s->n : s->body_ptr[b + 1] - s->body_ptr[b];
+        if (m <= lim) big = std::max(big, m);
+    }
+    if (big == 0) return 0;
+    const int cap = s->res_bin_req > 0 ? s->res_bin_req : (int)std::max<int64_t>(1024, big);
+    return std::min(lim, (cap + 31) & ~31);
 }
 
 // Builds the plan and all device buffers; positions/velocities come from the
@@ -390,6 +436,37 @@ int build_device(titan_gb300_sim *s) {
         max_heavy = std::max<int64_t>(max_heavy, ti.nheavy);
     }
     if (P.inc.size() > (size_t)INT32_MAX) return s->fail(TITAN_GB300_ELIMIT, "incidence table exceeds 2^31 words");
+    // body-resident bins: whole bodies that fit one CTA run all the steps of
+    // a launch in shared memory; the per-step kernels take the other tiles
+    s->use_res = false;
+    s->rplan = tg::ResPlan();
+    s->rargs = tg::ResArgs{};
+    {
+        const int cap = resident_cap(s);
+        if (cap > 0) {
+            tg::build_resident(in, P, cap, cap, s->rplan);
+            if (s->rplan.nbins > 0) {
+                s->use_res = true;
+                s->res_threads = s->res_threads_req > 0
+                                     ? s->res_threads_req
+                                     : std::max(128, std::min(512, ((cap + 1) / 2 + 31) & ~31));
+                const int mpt = (cap + s->res_threads - 1) / s->res_threads;
+                const size_t rsm = tg::resident_smem_bytes(s->prec, cap);
+                CK(tg::resident_prepare(s->prec, mpt, rsm), "set resident shared memory");
+                const int per_sm = tg::resident_ctas_per_sm(s->prec, mpt, s->res_threads, rsm);
+                if (per_sm <= 0) return s->fail(TITAN_GB300_ELIMIT, "resident bins do not fit one SM");
+                int sms = 0, dev = 0;
+                CK(cudaGetDevice(&dev), "device");
+                CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
+                s->res_ctas = (int)std::min<int64_t>(s->rplan.nbins, (int64_t)sms * per_sm);
+                s->rargs.nbins = s->rplan.nbins;
+                s->rargs.cap = cap;
+            }
+        }
+    }
+    std::vector<tg::TileInfo> tiles_run;
+    for (int64_t t = 0; t < P.ntiles; t++)
+        if (!s->use_res || !s->rplan.tile_resident[t]) tiles_run.push_back(tiles[t]);
     // shared-memory layout of the pipelined kernel (two stages)
     {
         auto al = [](int64_t x) { return (int32_t)((x + 15) & ~int64_t(15)); };
@@ -421,12 +498,12 @@ int build_device(titan_gb300_sim *s) {
         CK(cudaGetDevice(&dev), "device");
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
         per_sm = std::max(1, (227 * 1024) / a.pipe.total);
-        s->ctas = (int)std::min<int64_t>(P.ntiles, (int64_t)sms * per_sm);
+        s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), (int64_t)sms * per_sm);
     } else {
         if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
         CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
     }
-    a.ntiles = (int32_t)P.ntiles;
+    a.ntiles = (int32_t)tiles_run.size();
     if (P.ent_ends.size() > (size_t)INT32_MAX || P.halo.size() > (size_t)INT32_MAX)
         return s->fail(TITAN_GB300_ELIMIT, "more than 2^31 slab entries");
 #define DEVCOPY(dst, vec, what)                               \
@@ -435,7 +512,22 @@ int build_device(titan_gb300_sim *s) {
         if (!p_) return s->cuda_fail(e, what);                \
         dst = p_;                                             \
     } while (0)
-    DEVCOPY(a.tiles, tiles, "upload tiles");
+    DEVCOPY(a.tiles, tiles_run, "upload tiles");
+    if (s->use_res) {
+        tg::ResPlan &R = s->rplan;
+        tg::ResArgs &r = s->rargs;
+        DEVCOPY(r.bin_mass_off, R.bin_mass_off, "upload bins");
+        DEVCOPY(r.bin_warp_off, R.bin_warp_off, "upload bins");
+        DEVCOPY(r.mass, R.mass, "upload bins");
+        DEVCOPY(r.body, R.body, "upload bins");
+        DEVCOPY(r.deg, R.deg, "upload bins");
+        DEVCOPY(r.act_mask, R.act_mask, "upload bins");
+        DEVCOPY(r.warp_rec_off, R.warp_rec_off, "upload bins");
+        const size_t nrec = std::max<size_t>(1, R.words.size()) * (s->prec == P_FP64 ? 32 : 16);
+        if (!(r.rec = s->mem.get(nrec, e))) return s->cuda_fail(e, "alloc resident records");
+        if (!(r.act = s->mem.get(nrec, e))) return s->cuda_fail(e, "alloc resident records");
+        if (!(r.next = (int *)s->mem.get(sizeof(int), e))) return s->cuda_fail(e, "alloc bin queue");
+    }
     DEVCOPY(a.halo, P.halo, "upload halo");
     DEVCOPY(a.warp_inc_off, P.warp_inc_off, "upload warp offsets");
     std::vector<uint8_t> deg(np, 0);
@@ -636,9 +728,37 @@ int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
 int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
     if (!s || !out) return TITAN_GB300_EINVAL;
     out[0] = s->use_pipe ? 2 : 1;
-    out[1] = s->use_pipe ? s->ctas : s->plan.ntiles;
+    out[1] = s->use_pipe ? s->ctas : s->args.ntiles;
     out[2] = s->threads;
     out[3] = s->use_pipe ? s->args.pipe.total : (int64_t)s->smem;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int threads_per_cta) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (mode < 0 || mode > 1) return s->fail(TITAN_GB300_EINVAL, "resident mode must be 0 or 1");
+    if (bin_masses < 0 || bin_masses > 32767) return s->fail(TITAN_GB300_EINVAL, "bin size must be in [0, 32767]");
+    if (threads_per_cta != 0 && (threads_per_cta < 64 || threads_per_cta > 512 || threads_per_cta % 32))
+        return s->fail(TITAN_GB300_EINVAL, "threads per CTA must be 0 or a multiple of 32 in [64, 512]");
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "configure resident bins before start");
+    s->res_mode = mode;
+    s->res_bin_req = bin_masses;
+    s->res_threads_req = threads_per_cta;
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_resident_info(const titan_gb300_sim *s, int64_t out[8]) {
+    if (!s || !out) return TITAN_GB300_EINVAL;
+    std::memset(out, 0, 8 * sizeof(int64_t));
+    if (!s->use_res) return TITAN_GB300_OK;
+    out[0] = 1;
+    out[1] = s->rplan.nbins;
+    out[2] = s->rplan.nbodies;
+    out[3] = s->rplan.nmasses;
+    out[4] = s->rargs.cap;
+    out[5] = s->res_threads;
+    out[6] = s->res_ctas;
+    out[7] = (int64_t)tg::resident_smem_bytes(s->prec, s->rargs.cap);
     return TITAN_GB300_OK;
 }
 
@@ -649,6 +769,9 @@ int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
     tg::PlanInput in = plan_input(s, tile_masses);
     std::string why = tg::build_plan(in, s->plan);
     if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    s->rplan = tg::ResPlan();
+    const int cap = resident_cap(s);
+    if (cap > 0) tg::build_resident(in, s->plan, cap, cap, s->rplan);
     return TITAN_GB300_OK;
 }
 
@@ -678,6 +801,16 @@ int64_t titan_gb300_plan_table(const titan_gb300_sim *s, int table, void *out) {
         case TITAN_GB300_T_HEAVY_INC: return put(P.heavy_inc);
         case TITAN_GB300_T_BODY_OF_TILE: return put(P.body_of_tile);
         case TITAN_GB300_T_TILE_NH: return put(P.tile_nh);
+        case TITAN_GB300_T_RES_BIN_MASS_OFF: return put(s->rplan.bin_mass_off);
+        case TITAN_GB300_T_RES_BIN_WARP_OFF: return put(s->rplan.bin_warp_off);
+        case TITAN_GB300_T_RES_MASS: return put(s->rplan.mass);
+        case TITAN_GB300_T_RES_BODY: return put(s->rplan.body);
+        case TITAN_GB300_T_RES_DEG: return put(s->rplan.deg);
+        case TITAN_GB300_T_RES_ACT_MASK: return put(s->rplan.act_mask);
+        case TITAN_GB300_T_RES_WARP_REC_OFF: return put(s->rplan.warp_rec_off);
+        case TITAN_GB300_T_RES_WORDS: return put(s->rplan.words);
+        case TITAN_GB300_T_RES_REC_SPRING: return put(s->rplan.rec_spring);
+        case TITAN_GB300_T_RES_RESIDENT: return put(s->rplan.resident);
         default: return -1;
     }
 }
@@ -867,6 +1000,16 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
     if (nsteps == 0) return TITAN_GB300_OK;
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
     cudaError_t e = cudaSuccess;
+    if (s->use_res)
+        CK(tg::launch_resident(s->prec, s->args, s->rargs, s->res_ctas, s->res_threads, s->parity, nsteps, 1,
+                               s->args.ntiles == 0, s->stream),
+           "launch resident bins");
+    if (s->args.ntiles == 0) {
+        s->parity ^= (int)(nsteps & 1);
+        for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
+        s->steps += nsteps;
+        return TITAN_GB300_OK;
+    }
     int64_t rem = nsteps - 1;
     while (rem > 0) {
         int len = (int)std::min<int64_t>(rem, kChunk);
@@ -1084,6 +1227,11 @@ int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64
             int64_t j = s->plan.ent_spring[e];
             s->plan.ent_ends[e] = (s->plan.ent_ends[e] & 0x00ffffffu) | ((uint32_t)(s->type[j] & 3) << 24);
         }
+        if (s->use_res)
+            for (size_t q = 0; q < s->rplan.words.size(); q++) {
+                int64_t j = s->rplan.rec_spring[q];
+                if (j >= 0) s->rplan.words[q] = (s->rplan.words[q] & 0xffffu) | ((uint32_t)(s->type[j] & 3) << 16);
+            }
     }
     return upload_entries(s);
 }

@@ -89,6 +89,25 @@ struct StepArgs {
     PipeLayout pipe;
 };
 
+// Body-resident batched launch (resident.cu, plan.h ResPlan): bins of whole
+// bodies, each run by one CTA for all steps of a launch with its state in
+// shared memory.  Records use the slab-entry layout (entry_record_bytes)
+// with the entry word replaced by the resident word.
+struct ResArgs {
+    const int64_t *bin_mass_off;   // nbins+1
+    const int64_t *bin_warp_off;   // nbins+1
+    const int32_t *mass;           // tiled index per resident mass
+    const int32_t *body;
+    const uint8_t *deg;
+    const uint64_t *act_mask;
+    const uint32_t *warp_rec_off;
+    const void *rec;
+    const void *act;
+    int *next;                     // bin queue counter, zero at launch
+    int64_t nbins;
+    int32_t cap;                   // masses per bin (shared memory holds 2 * cap records)
+};
+
 // Per-mass gather / scatter between caller order and tiled order.
 struct XferArgs {
     const int32_t *old2new;
@@ -132,6 +151,14 @@ cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int thr
 // bytes of one state record / one slab entry record for a precision
 int state_record_bytes(int precision);
 int entry_record_bytes(int precision);
+// Resident launch: `nsteps` steps of every bin, starting from parity;
+// masses per thread = ceil(cap / threads) must be at most kResMaxMpt.
+constexpr int kResMaxMpt = 4;
+size_t resident_smem_bytes(int precision, int cap);
+cudaError_t resident_prepare(int precision, int mpt, size_t smem);
+int resident_ctas_per_sm(int precision, int mpt, int threads, size_t smem);
+cudaError_t launch_resident(int precision, const StepArgs &a, const ResArgs &r, int ctas, int threads, int parity,
+                            int64_t nsteps, int write_acc, int write_time, cudaStream_t s);
 cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_scatter(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_diag(int precision, const DiagArgs &a, cudaStream_t s);

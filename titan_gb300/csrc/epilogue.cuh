@@ -16,7 +16,8 @@ template <int PREC>
 __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti, int64_t g, uint8_t fl,
                                           typename Real<PREC>::T m, typename Real<PREC>::T F0,
                                           typename Real<PREC>::T F1, typename Real<PREC>::T F2, St<PREC> &s,
-                                          void *out, int write_acc, int64_t np, const DevParams *prm) {
+                                          void *out, int64_t gs, int write_acc, int64_t np,
+                                          const DevParams *prm) {
     if constexpr (PREC == P_FP64) {
         double Fd[3] = {F0, F1, F2};
         Fd[0] = Fd[0] + prm->g[0] * m;
@@ -54,7 +55,7 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
             s.v[c] = s.v[c] + acc[c] * dt;
             s.x[c] = s.x[c] + s.v[c] * dt;
         }
-        store_state<PREC>(out, g, s);
+        store_state<PREC>(out, gs, s);
         if (write_acc) {
             double *ac = reinterpret_cast<double *>(a.acc);
             ac[g] = acc[0];
@@ -133,7 +134,7 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
                 s.x[c] = s.x[c] + s.v[c] * prm->dt_hi;
             }
         }
-        store_state<PREC>(out, g, s);
+        store_state<PREC>(out, gs, s);
         if (write_acc) {
             float *ac = reinterpret_cast<float *>(a.acc);
             ac[g] = acc[0];

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <deque>
+#include <map>
 #include <numeric>
 #include <utility>
 
@@ -249,6 +250,136 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
     P.ntiles = (int64_t)P.body_of_tile.size();
     return "";
+}
+
+void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_cap, ResPlan &R) {
+    R = ResPlan();
+    const int64_t n = P.n;
+    std::vector<int64_t> bptr;
+    if (in.nbodies > 0 && in.body_ptr)
+        bptr.assign(in.body_ptr, in.body_ptr + in.nbodies + 1);
+    else
+        bptr = {0, n};
+    const int64_t nb = (int64_t)bptr.size() - 1;
+    R.resident.assign(nb, 0);
+    R.tile_resident.assign(P.ntiles, 0);
+    max_masses = std::min(max_masses, 32767);
+    bin_cap = std::max(std::min(bin_cap, 32767), 1);
+    max_masses = std::min(max_masses, bin_cap);
+    R.bin_cap = bin_cap;
+    auto fixed_new = [&](int64_t g) { return in.fixed && in.fixed[P.new2old[g]]; };
+    // bodies occupy contiguous ranges of the tiled order (tiles never
+    // straddle bodies and masses are only reordered inside a body)
+    std::vector<int32_t> body_of(n);
+    for (int64_t b = 0; b < nb; b++)
+        for (int64_t g = bptr[b]; g < bptr[b + 1]; g++) body_of[g] = (int32_t)b;
+    // incidence of each free mass in the new numbering, ascending springs
+    std::vector<int64_t> ip(n + 1, 0);
+    std::vector<uint8_t> cross(nb, 0);
+    for (int64_t s = 0; s < in.ns; s++) {
+        int32_t l = in.left[s], r = in.right[s];
+        if (l < 0 || r < 0 || l >= n || r >= n) continue;
+        int64_t L = P.old2new[l], Rr = P.old2new[r];
+        if (body_of[L] != body_of[Rr]) cross[body_of[L]] = cross[body_of[Rr]] = 1;
+        if (!fixed_new(Rr)) ip[Rr + 1]++;
+        if (!fixed_new(L)) ip[L + 1]++;
+    }
+    for (int64_t i = 0; i < n; i++) ip[i + 1] += ip[i];
+    std::vector<int64_t> isp(ip[n]), iother(ip[n]);
+    std::vector<int8_t> iright(ip[n]);
+    {
+        std::vector<int64_t> fill(ip.begin(), ip.end() - 1);
+        for (int64_t s = 0; s < in.ns; s++) {
+            int32_t l = in.left[s], r = in.right[s];
+            if (l < 0 || r < 0 || l >= n || r >= n) continue;
+            int64_t L = P.old2new[l], Rr = P.old2new[r];
+            if (!fixed_new(Rr)) { isp[fill[Rr]] = s; iother[fill[Rr]] = L; iright[fill[Rr]] = 1; fill[Rr]++; }
+            if (!fixed_new(L)) { isp[fill[L]] = s; iother[fill[L]] = Rr; iright[fill[L]] = 0; fill[L]++; }
+        }
+    }
+    // eligible bodies, largest first (ties: body order)
+    std::vector<int64_t> elig;
+    for (int64_t b = 0; b < nb; b++) {
+        const int64_t nm = bptr[b + 1] - bptr[b];
+        if (nm > max_masses || cross[b]) continue;
+        bool ok = true;
+        for (int64_t g = bptr[b]; g < bptr[b + 1] && ok; g++) ok = ip[g + 1] - ip[g] <= 254;
+        if (ok) elig.push_back(b);
+    }
+    std::stable_sort(elig.begin(), elig.end(),
+                     [&](int64_t a, int64_t b) { return bptr[a + 1] - bptr[a] > bptr[b + 1] - bptr[b]; });
+    // best fit: the fullest bin the body still fits in
+    std::multimap<int64_t, int64_t> room;  // remaining capacity -> bin
+    std::vector<std::vector<int64_t>> bins;
+    for (int64_t b : elig) {
+        const int64_t nm = bptr[b + 1] - bptr[b];
+        auto it = room.lower_bound(nm);
+        int64_t k;
+        if (it == room.end()) {
+            k = (int64_t)bins.size();
+            bins.emplace_back();
+        } else {
+            k = it->second;
+            room.erase(it);
+        }
+        bins[k].push_back(b);
+        int64_t used = 0;
+        for (int64_t q : bins[k]) used += bptr[q + 1] - bptr[q];
+        if (bin_cap - used > 0) room.emplace(bin_cap - used, k);
+        R.resident[b] = 1;
+    }
+    // bins with the most incidence work first
+    std::vector<int64_t> work(bins.size(), 0), order(bins.size());
+    for (size_t k = 0; k < bins.size(); k++)
+        for (int64_t b : bins[k]) work[k] += ip[bptr[b + 1]] - ip[bptr[b]] + (bptr[b + 1] - bptr[b]);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return work[a] > work[b]; });
+    R.nbins = (int64_t)bins.size();
+    R.bin_mass_off.push_back(0);
+    R.bin_warp_off.push_back(0);
+    std::vector<int64_t> local(n, -1);
+    for (int64_t k : order) {
+        const int64_t m0 = (int64_t)R.mass.size();
+        for (int64_t b : bins[k]) {
+            R.nbodies++;
+            for (int64_t g = bptr[b]; g < bptr[b + 1]; g++) {
+                local[g] = (int64_t)R.mass.size() - m0;
+                R.mass.push_back((int32_t)g);
+                R.body.push_back((int32_t)b);
+            }
+        }
+        const int64_t m1 = (int64_t)R.mass.size();
+        for (int64_t w0 = m0; w0 < m1; w0 += 32) {
+            const int64_t w1 = std::min(w0 + 32, m1);
+            int64_t width = 0;
+            for (int64_t q = w0; q < w1; q++) {
+                const int64_t g = R.mass[q];
+                width = std::max(width, ip[g + 1] - ip[g]);
+            }
+            const uint32_t off = (uint32_t)R.words.size();
+            R.warp_rec_off.push_back(off);
+            R.words.resize(R.words.size() + (size_t)(width * 32), 0);
+            R.rec_spring.resize(R.words.size(), -1);
+            for (int64_t q = w0; q < w1; q++) {
+                const int64_t g = R.mass[q], lane = q - w0, d = ip[g + 1] - ip[g];
+                uint64_t mask = 0;
+                for (int64_t j = 0; j < d; j++) {
+                    const int64_t e = ip[g] + j, s = isp[e];
+                    const uint32_t other = (uint32_t)local[iother[e]];
+                    const uint32_t ty = in.type ? (uint32_t)in.type[s] & 3u : 0u;
+                    R.words[off + j * 32 + lane] = other | (iright[e] ? 0x8000u : 0u) | (ty << 16);
+                    R.rec_spring[off + j * 32 + lane] = s;
+                    if (j < 64 && ty >= 2) mask |= uint64_t(1) << j;
+                }
+                R.deg.push_back((uint8_t)d);
+                R.act_mask.push_back(mask);
+            }
+        }
+        R.bin_mass_off.push_back(m1);
+        R.bin_warp_off.push_back((int64_t)R.warp_rec_off.size());
+    }
+    R.nmasses = (int64_t)R.mass.size();
+    for (int64_t t = 0; t < P.ntiles; t++) R.tile_resident[t] = R.resident[P.body_of_tile[t]];
 }
 
 }  // namespace tg

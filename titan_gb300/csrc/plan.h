@@ -77,4 +77,35 @@ struct Plan {
 // not fit one tile's slab).
 std::string build_plan(const PlanInput &in, Plan &out);
 
+// Body-resident plan: bodies small enough for one CTA keep their state in
+// shared memory for a whole multi-step launch.  Whole bodies are packed into
+// bins of at most bin_cap masses (best fit, largest body first); one CTA
+// runs one bin at a time.  Each bin-local mass lists its springs in
+// ascending order as records whose word is
+//   other end's bin-local index | 0x8000 if this mass is the right end |
+//   type << 16
+// laid out per warp of 32 bin-local masses as ELL: record j of lane l of
+// bin warp w is warp_rec_off[w] + 32 j + l.
+struct ResPlan {
+    int64_t nbins = 0;
+    int bin_cap = 0;
+    std::vector<int64_t> bin_mass_off;   // nbins+1, into the per-resident-mass arrays
+    std::vector<int64_t> bin_warp_off;   // nbins+1, into warp_rec_off
+    std::vector<int32_t> mass;           // tiled index of each resident mass (bin order)
+    std::vector<int32_t> body;           // its body
+    std::vector<uint8_t> deg;            // its degree (free masses; 0 if fixed)
+    std::vector<uint64_t> act_mask;      // bit j: record j (j < 64) is actuated
+    std::vector<uint32_t> warp_rec_off;  // first record of each bin warp
+    std::vector<uint32_t> words;         // one per record (padding: 0)
+    std::vector<int64_t> rec_spring;     // spring of each record, -1 = padding
+    std::vector<uint8_t> resident;       // per body: 1 if resident
+    std::vector<uint8_t> tile_resident;  // per tile of Plan: 1 if it belongs to a resident body
+    int64_t nmasses = 0, nbodies = 0;
+};
+
+// Picks the bodies with at most max_masses masses, no mass of degree above
+// 254 (free masses only count) and no spring to another body, and packs
+// them into bins of bin_cap masses (bin_cap >= max_masses).
+void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_cap, ResPlan &R);
+
 }  // namespace tg

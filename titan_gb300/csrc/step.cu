@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_
             }
         }
         St<PREC> s = load_state_smem<PREC>(st, i);
-        integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, s, out, write_acc, np, prm);
+        integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, s, out, g, write_acc, np, prm);
     }
 }
 

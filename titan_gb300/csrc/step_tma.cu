@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
                 for (uint32_t w = 0; w < nw; w++) gather_word<PREC>(recb, ip[32 * w], w, d, F0, F1, F2);
             }
             St<PREC> sv = load_state_smem<PREC>(st, i);
-            integrate<PREC>(a, ti, g, fli, mi, F0, F1, F2, sv, out, write_acc, np, prm);
+            integrate<PREC>(a, ti, g, fli, mi, F0, F1, F2, sv, out, g, write_acc, np, prm);
         }
         __syncthreads();  // the stage and the index buffer are free again
     }

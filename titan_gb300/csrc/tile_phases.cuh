@@ -75,16 +75,20 @@ __device__ __forceinline__ Rec16<PREC> ldg_rec(const uint8_t *p) {  // read-only
     return r;
 }
 
-// Force of a slab entry (record rec; actuation record act when actuated) on
-// its right end, from the state records staged at st; written to slot.
 template <int PREC>
-__device__ __forceinline__ void entry_force(const Rec16<PREC> &rec, bool actuated, const Rec16<PREC> &act,
-                                            const uint8_t *st, const StepTime &t, uint8_t *slot) {
+struct F3 {
+    typename Real<PREC>::T x, y, z;
+};
+
+// Force on the right end of a spring whose ends are the state records sa
+// (left) and sb (right) staged at st; k, rest, damping from the spring's
+// record, type from its entry word, act its actuation record.
+template <int PREC>
+__device__ __forceinline__ F3<PREC> spring_force(int sa, int sb, uint32_t type, typename Real<PREC>::T k,
+                                                 typename Real<PREC>::T rest, typename Real<PREC>::T damping,
+                                                 bool actuated, const Rec16<PREC> &act, const uint8_t *st,
+                                                 const StepTime &t) {
     if constexpr (PREC == P_FP64) {
-        const double2 r01 = rec.lo;
-        const double2 r23 = rec.hi;
-        const uint32_t ends = (uint32_t)__double_as_longlong(r23.y);
-        const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
         double scale = 1.0;
         if (actuated) {
             const double2 q01 = act.lo;
@@ -92,7 +96,7 @@ __device__ __forceinline__ void entry_force(const Rec16<PREC> &rec, bool actuate
             double th = q01.x * t.T;
             th = th + q23.x;
             const double sn = q01.y * sin(th);
-            scale = ((ends >> 24) & 3) == 2 ? 1.0 - sn : 1.0 + sn;
+            scale = type == 2 ? 1.0 - sn : 1.0 + sn;
         }
         const double2 *pa = reinterpret_cast<const double2 *>(st + (int64_t)sa * 48);
         const double2 *pb = reinterpret_cast<const double2 *>(st + (int64_t)sb * 48);
@@ -100,28 +104,25 @@ __device__ __forceinline__ void entry_force(const Rec16<PREC> &rec, bool actuate
         const double d0 = b0.x - a0.x, d1 = b0.y - a0.y, d2 = b1.x - a1.x;
         const double nrm = nrm3(d0, d1, d2);
         const double u0 = d0 / nrm, u1 = d1 / nrm, u2 = d2 / nrm;
-        const double fs = r01.x * (r01.y * scale - nrm);
+        const double fs = k * (rest * scale - nrm);
         double f0 = u0 * fs, f1 = u1 * fs, f2 = u2 * fs;
-        if (r23.x != 0.0) {
+        if (damping != 0.0) {
             const double2 a2 = pa[2], b2 = pb[2];
             const double w0 = a1.y - b1.y, w1 = a2.x - b2.x, w2 = a2.y - b2.y;
-            const double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * r23.x;
+            const double dd = ((w0 * u0 + w1 * u1) + w2 * u2) * damping;
             f0 = f0 + u0 * dd;
             f1 = f1 + u1 * dd;
             f2 = f2 + u2 * dd;
         }
-        reinterpret_cast<double2 *>(slot)[0] = make_double2(f0, f1);
-        reinterpret_cast<double2 *>(slot)[1] = make_double2(f2, 0.0);
+        return F3<PREC>{f0, f1, f2};
     } else {
-        const float4 r = rec.v;
-        const uint32_t ends = __float_as_uint(r.x);
-        const int sa = ends & 0xfff, sb = (ends >> 12) & 0xfff;
-        float rs = r.z;
+        (void)type;
+        float rs = rest;
         if (actuated) {
             const float4 q = act.v;
             const float cyc = fmaf(q.x, t.hi, fmaf(q.x, t.lo, q.z));
             const float fr = cyc - rintf(cyc);
-            rs = r.z * fmaf(q.y, __sinf(6.28318530717958647692f * fr), 1.0f);
+            rs = rest * fmaf(q.y, __sinf(6.28318530717958647692f * fr), 1.0f);
         }
         constexpr int kV = PREC == P_FP32 ? 2 : 3;  // float4 per state record
         const float4 *pa = reinterpret_cast<const float4 *>(st) + sa * kV;
@@ -138,13 +139,32 @@ __device__ __forceinline__ void entry_force(const Rec16<PREC> &rec, bool actuate
         float rq = rsqrtf(n2);
         rq = rq * fmaf(-0.5f * n2 * rq, rq, 1.5f);  // one Newton step
         const float nrm = n2 * rq;
-        float f = r.y * (rs - nrm);
-        if (r.w != 0.f) {
+        float f = k * (rs - nrm);
+        if (damping != 0.f) {
             const float w0 = a0.w - b0.w, w1 = a1.x - b1.x, w2 = a1.y - b1.y;
-            f = fmaf(fmaf(w2, d2, fmaf(w1, d1, w0 * d0)), rq * r.w, f);
+            f = fmaf(fmaf(w2, d2, fmaf(w1, d1, w0 * d0)), rq * damping, f);
         }
         const float fr = f * rq;
-        *reinterpret_cast<float4 *>(slot) = make_float4(d0 * fr, d1 * fr, d2 * fr, 0.f);
+        return F3<PREC>{d0 * fr, d1 * fr, d2 * fr};
+    }
+}
+
+// Force of a slab entry (record rec; actuation record act when actuated) on
+// its right end, from the state records staged at st; written to slot.
+template <int PREC>
+__device__ __forceinline__ void entry_force(const Rec16<PREC> &rec, bool actuated, const Rec16<PREC> &act,
+                                            const uint8_t *st, const StepTime &t, uint8_t *slot) {
+    if constexpr (PREC == P_FP64) {
+        const uint32_t ends = (uint32_t)__double_as_longlong(rec.hi.y);
+        const F3<PREC> f = spring_force<PREC>(ends & 0xfff, (ends >> 12) & 0xfff, (ends >> 24) & 3, rec.lo.x,
+                                              rec.lo.y, rec.hi.x, actuated, act, st, t);
+        reinterpret_cast<double2 *>(slot)[0] = make_double2(f.x, f.y);
+        reinterpret_cast<double2 *>(slot)[1] = make_double2(f.z, 0.0);
+    } else {
+        const uint32_t ends = __float_as_uint(rec.v.x);
+        const F3<PREC> f = spring_force<PREC>(ends & 0xfff, (ends >> 12) & 0xfff, (ends >> 24) & 3, rec.v.y,
+                                              rec.v.z, rec.v.w, actuated, act, st, t);
+        *reinterpret_cast<float4 *>(slot) = make_float4(f.x, f.y, f.z, 0.f);
     }
 }
 
