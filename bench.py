@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--threads", type=int, default=0)
     p.add_argument("--kernel", type=int, default=0, help="0 auto, 1 per-tile, 2 pipelined")
+    p.add_argument("--ref-gpu-steps", type=int, default=50,
+                   help="steps of the reference's own CUDA kernels timed beside ours (0: skip)")
     return p.parse_args()
 
 
@@ -141,6 +143,33 @@ def cpu_oracle_rate(sc, steps, threads):
     o.step(steps, po.ATOMIC_OMP, threads)
     dt = time.perf_counter() - t0
     return sc["left"].size * steps / dt, dt
+
+
+def reference_kernels(sc, steps, device, value, fp64):
+    """The reference's own CUDA kernels (computeSpringForces +
+    massForcesAndUpdate, compiled from its sources) on the same scene and
+    GPU: back to back (kernel-only) and with execute()'s per-step device
+    synchronisation."""
+    from oracle import refgpu
+    why = refgpu.available()
+    if why:
+        return {"unavailable": why}
+    ns = sc["left"].size
+    r = refgpu.RefGpuSim(sc, device)
+    try:
+        r.step(3)
+        ms = r.time_steps(steps)
+        ms_sync = r.time_steps(max(1, steps // 2), sync_each=True) / max(1, steps // 2) * steps
+    finally:
+        r.close()
+    out = {"value": ns * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+           "ms_per_step_with_step_sync": ms_sync / steps, "steps": steps, "dtype": "f64",
+           "speedup_of_headline": value / (ns * steps / (ms / 1e3)),
+           "note": "reference src/sim.cu kernels, 1024-thread blocks, FP64 atomics; actuation at the reference's "
+                   "fixed 0.2 amplitude (same actuated springs and omegas)"}
+    if fp64:
+        out["speedup_of_fp64"] = fp64["value"] / out["value"]
+    return out
 
 
 def run_ours(a, rank, world, local):
@@ -233,6 +262,10 @@ def run_ours(a, rank, world, local):
                 "note": "FP64 drop-in (bit-identical to the CPU oracle); FP64-ALU bound on GB300"}
         s64.close()
 
+    ref_gpu = None
+    if rank == 0 and world == 1 and a.ref_gpu_steps > 0:
+        ref_gpu = reference_kernels(sc, a.ref_gpu_steps, local, value, fp64)
+
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -270,6 +303,8 @@ def run_ours(a, rank, world, local):
     }
     if fp64:
         res["fp64"] = fp64
+    if ref_gpu:
+        res["reference_kernels"] = ref_gpu
     if cpu:
         res["cpu_baseline"] = cpu
     return res

@@ -124,6 +124,10 @@ def build_reference_pieces(verbose: bool = False) -> Path | None:
     script = ORACLE / "build_ref.sh"
     if not Path("/root/reference/src/object.cu").exists() or not script.exists():
         return None
+    out = ORACLE / "_ref" / "libtitan_ref_host.so"
+    deps = [script, ORACLE / "ref_host_shim.cu", ORACLE / "ref_gpu_shim.cu", *(ORACLE / "ref_shims").glob("*.h")]
+    if not _stale(out, deps) and not _stale(ORACLE / "_ref" / "titan_ref_kernels.cubin", deps):
+        return out
     r = subprocess.run(["bash", str(script)], capture_output=True, text=True)
     if r.returncode != 0:
         if verbose:
@@ -133,10 +137,25 @@ def build_reference_pieces(verbose: bool = False) -> Path | None:
     return out if out.exists() else None
 
 
+def build_ref_gpu_harness(verbose: bool = False) -> Path:
+    """Compile the driver-API harness that runs the reference's own kernels
+    from oracle/_ref/titan_ref_kernels.cubin (test infrastructure only; needs
+    no reference file, so it builds wherever the CUDA toolkit is)."""
+    src = ORACLE / "ref_gpu_harness.cpp"
+    out = ORACLE / "libref_gpu_harness.so"
+    cuda = Path(_nvcc()).resolve().parent.parent
+    if _stale(out, [src]):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", str(cuda / "include"), str(src),
+              "-o", str(out), "-L", str(cuda / "lib64"), "-L", str(cuda / "lib64" / "stubs"), "-lcuda"])
+    if verbose:
+        print("built", out)
+    return out
+
+
 def build_all(verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         futs = [ex.submit(build_library, verbose), ex.submit(build_oracle, verbose),
-                ex.submit(build_reference_pieces, verbose)]
+                ex.submit(build_reference_pieces, verbose), ex.submit(build_ref_gpu_harness, verbose)]
         for f in futs:
             f.result()
 
