@@ -143,14 +143,24 @@ int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
  * tile size itself is start()'s argument.  Used by the autotuner. */
 int titan_gb300_set_launch(titan_gb300_sim *sim, int threads_per_cta);
 
+/* Register cap of the per-tile step kernel in the FP32 forms: 0 or 1 = none
+ * (up to 128 registers per thread), 3 or 4 = compile-time launch bounds for
+ * 3 or 4 resident CTAs per SM of at most 256 threads (85 / 64 registers).
+ * More resident warps hide more memory latency; fewer registers may spill.
+ * FP64 ignores it.  Set before start(); start() fails with EINVAL when the
+ * CTA is larger than 256 threads.  Used by the autotuner. */
+int titan_gb300_set_occupancy(titan_gb300_sim *sim, int min_ctas_per_sm);
+
 /* Step kernel form: 0 = automatic (currently the per-tile kernel, the faster
  * form measured on GB300), 1 = per-tile kernel (one CTA per tile), 2 =
  * pipelined persistent kernel (TMA-staged tiles; fails at start() when two
- * tiles do not fit in shared memory).  Both forms give bit-identical
- * results.  Set before start(). */
+ * tiles do not fit in shared memory), 3 = per-tile kernel whose slab records
+ * and tile states arrive by bulk copy (TMA) and halo by cp.async, all issued
+ * before one wait.  All forms give bit-identical results.  Set before
+ * start(). */
 int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
 
-/* After start(): out[0] kernel form in use (1 or 2), out[1] CTAs per launch,
+/* After start(): out[0] kernel form in use (1, 2 or 3), out[1] CTAs per launch,
  * out[2] threads per CTA, out[3] dynamic shared memory per CTA (bytes). */
 int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
 

@@ -309,3 +309,13 @@ def test_set_resident_validates():
     s.set_resident(1, 512, 128)
     s.set_resident(0)
     s.close()
+
+
+def test_set_occupancy_validates():
+    s = tg.Sim(tg.FP32C)
+    for v in (-1, 2, 5):
+        with pytest.raises(tg.TitanError, match="EINVAL"):
+            s.set_occupancy(v)
+    s.set_occupancy(4)
+    s.set_occupancy(0)
+    s.close()

@@ -154,25 +154,33 @@ def kernel_scenes():
 @pytest.mark.parametrize("scene", ["lattice", "hub", "bodies"])
 @pytest.mark.parametrize("tile", [32, 96])
 def test_kernel_forms_bitwise_identical(precision, scene, tile):
-    """The pipelined persistent kernel (TMA-staged tiles) and the per-tile
-    kernel give identical bits in every precision."""
+    """The pipelined persistent kernel (TMA-staged tiles), the per-tile
+    kernel and the per-tile kernel with asynchronous staging give identical
+    bits in every precision."""
     sc = kernel_scenes()[scene]
     s1, a = gpu_run(sc, 700, precision, tile=tile, kernel=1, resident=(0, 0, 0))
     s2, b = gpu_run(sc, 700, precision, tile=tile, kernel=2, resident=(0, 0, 0))
+    s3, c = gpu_run(sc, 700, precision, tile=tile, kernel=3, resident=(0, 0, 0))
+    s4, d = gpu_run(sc, 700, precision, tile=tile, kernel=4, resident=(0, 0, 0))
     assert s1.kernel_info()["kernel"] == "per-tile" and s2.kernel_info()["kernel"] == "pipelined"
+    assert s3.kernel_info()["kernel"] == "per-tile-async" and s4.kernel_info()["kernel"] == "warp-specialised"
     for k in ("pos", "vel", "acc", "T"):
         assert np.array_equal(a[k], b[k]), k
+        assert np.array_equal(a[k], c[k]), k
+        assert np.array_equal(a[k], d[k]), k
 
 
 def test_pipelined_kernel_with_few_ctas_per_tile_list():
-    """Tiles walked by a persistent grid: more tiles than CTAs, odd counts."""
+    """Tiles walked by a persistent grid (pipelined and warp-specialised
+    forms): more tiles than CTAs, odd counts."""
     sc = wl.lattice_scene((0, 0, 1.0), (2, 2, 2), 41, 39, 37, k=3e3, damping=0.1)
     sc["planes"].append(((0.0, 0.0, 1.0), 0.0, 0.5, 0.5))
     _, a = gpu_run(sc, 300, tg.FP64, tile=32, kernel=1)
-    s, b = gpu_run(sc, 300, tg.FP64, tile=32, kernel=2)
-    info = s.kernel_info()
-    assert info["ctas"] < s.plan_info()["tiles"]
-    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    for form in (2, 4):
+        s, b = gpu_run(sc, 300, tg.FP64, tile=32, kernel=form)
+        info = s.kernel_info()
+        assert info["ctas"] < s.plan_info()["tiles"]
+        assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
 def test_graph_chunks_equal_single_steps_and_repeatable():
@@ -305,3 +313,16 @@ def test_full_size_config2_fp32c_vs_fp64_200_steps():
     err = np.max(np.abs(a["pos"] - b["pos"]))
     print(f"100^3 fp32c vs fp64 after 200 steps: {err:.3e} m")
     assert err < 1e-6
+
+
+@pytest.mark.parametrize("precision", [tg.FP32, tg.FP32C])
+@pytest.mark.parametrize("occupancy", [3, 4])
+def test_register_capped_variants_bitwise_identical(precision, occupancy):
+    """Launch-bound variants of the per-tile kernel compute the same bits."""
+    sc = kernel_scenes()["lattice"]
+    _, a = gpu_run(sc, 500, precision, tile=64, threads=128, kernel=1)
+    s = wl.make_sim(sc, precision, 64, threads=128, kernel=1, occupancy=occupancy)
+    s.step(500)
+    b = s.get_state(acc=True, T=True)
+    for k in ("pos", "vel", "acc", "T"):
+        assert np.array_equal(a[k], b[k]), k

@@ -62,6 +62,7 @@ _SIGS = {
     "titan_gb300_start": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_launch": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_kernel": (ctypes.c_int, [_P, ctypes.c_int]),
+    "titan_gb300_set_occupancy": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_kernel_info": (ctypes.c_int, [_P, _I64]),
     "titan_gb300_set_resident": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "titan_gb300_resident_info": (ctypes.c_int, [_P, _I64]),
@@ -252,14 +253,22 @@ class Sim:
     def set_launch(self, threads_per_cta: int):
         self._check(self._L.titan_gb300_set_launch(self._h, threads_per_cta), "set_launch")
 
+    def set_occupancy(self, min_ctas_per_sm: int):
+        """Register cap of the per-tile kernel (FP32 forms): 0 none, 3 or 4
+        resident CTAs per SM (at most 256 threads per CTA)."""
+        self._check(self._L.titan_gb300_set_occupancy(self._h, min_ctas_per_sm), "set_occupancy")
+
     def set_kernel(self, variant: int):
-        """0 automatic, 1 per-tile kernel, 2 pipelined persistent kernel."""
+        """0 automatic, 1 per-tile kernel, 2 pipelined persistent kernel, 3 per-tile
+        kernel with asynchronous (bulk-copy) staging, 4 warp-specialised
+        persistent kernel (producer warp + consumer warps, stage ring)."""
         self._check(self._L.titan_gb300_set_kernel(self._h, variant), "set_kernel")
 
     def kernel_info(self) -> dict:
         out = np.zeros(4, np.int64)
         self._check(self._L.titan_gb300_kernel_info(self._h, _ptr(out, ctypes.c_int64)), "kernel_info")
-        return {"kernel": "pipelined" if out[0] == 2 else "per-tile", "ctas": int(out[1]), "threads": int(out[2]),
+        names = {1: "per-tile", 2: "pipelined", 3: "per-tile-async", 4: "warp-specialised"}
+        return {"kernel": names.get(int(out[0]), "per-tile"), "ctas": int(out[1]), "threads": int(out[2]),
                 "smem_bytes": int(out[3])}
 
     def set_resident(self, mode: int = 1, bin_masses: int = 0, threads: int = 0):

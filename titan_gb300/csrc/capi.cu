@@ -106,8 +106,13 @@ struct titan_gb300_sim {
     size_t rsize() const { return prec == P_FP64 ? sizeof(double) : sizeof(float); }
     int comps() const { return tg::state_words(prec); }
     int threads_req = 0;  // CTA size override (0: derived from the tile size)
-    int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 2 pipelined kernel
+    int min_ctas_req = 0; // register cap of the per-tile kernel: 0/1 none, 3 or 4 CTAs per SM
+    int step_variant = 0; // launch-bound variant in use (engine.h)
+    int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 2 pipelined kernel, 3 per-tile with async staging
     bool use_pipe = false;
+    bool use_async = false;
+    bool use_ws = false;
+    int ws_warps = 0;     // consumer warps of the warp-specialised kernel
     int ctas = 0;         // persistent grid of the pipelined kernel
     int *d_err = nullptr;
     // body-resident batched launch
@@ -122,7 +127,11 @@ struct titan_gb300_sim {
     cudaError_t launch(int parity, int write_acc) {
         if (args.ntiles == 0) return cudaSuccess;
         if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
-        return tg::launch_step(prec, args, (int)args.ntiles, threads, smem, parity, write_acc, stream);
+        if (use_ws) return tg::launch_step_ws(prec, args, ctas, ws_warps, parity, write_acc, stream);
+        if (use_async)
+            return tg::launch_step_async(prec, args, (int)args.ntiles, threads, smem, parity, write_acc, stream);
+        return tg::launch_step(prec, step_variant, args, (int)args.ntiles, threads, smem, parity, write_acc,
+                               stream);
     }
 
     int fail(int code, const std::string &msg) {
@@ -350,7 +359,11 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : 256);
+    // default tile: 128 masses in FP64; in the FP32 forms 192 for the
+    // warp-specialised kernel (two stages fit one SM's shared memory) and 256
+    // for the per-tile forms (measured fastest on GB300, see profiles/)
+    const bool ws = s->kernel_req == 0 || s->kernel_req == 4;
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : (ws ? 192 : 256));
     in.heavy_threshold = 96;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)
@@ -427,7 +440,9 @@ int build_device(titan_gb300_sim *s) {
         ti.inc_off = (int32_t)i0;
         ti.inc_words = (int32_t)(i1 - i0);
         ti.pad0 = ti.pad1 = ti.pad2 = 0;
-        s->smem = std::max(s->smem, tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy));
+        s->smem = std::max(s->smem, s->kernel_req == 3
+                                        ? tg::tile_async_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy)
+                                        : tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy));
         max_ne = std::max<int64_t>(max_ne, ti.ne);
         max_nact = std::max<int64_t>(max_nact, ti.nact);
         max_incw = std::max<int64_t>(max_incw, ti.inc_words);
@@ -484,8 +499,58 @@ int build_device(titan_gb300_sim *s) {
         L.tinfo = L.mbar + 16;
         L.total = L.tinfo + tg::kPipeTileCache * (int32_t)sizeof(tg::TileInfo);
     }
-    // automatic choice: the per-tile form (measured faster on GB300 for the
-    // lattice workloads, see the kernel-form sweep in profiles/)
+    // automatic choice: the warp-specialised form in FP32 and FP32C (measured
+    // fastest on GB300, see the kernel-form sweep in profiles/) when two of
+    // the scene's tiles fit one SM's shared memory, else the per-tile form;
+    // the per-tile form in FP64 (FP64-ALU bound, no gain from overlap)
+    s->use_ws = false;
+    const bool want_ws = s->kernel_req == 4 || (s->kernel_req == 0 && s->prec != P_FP64 && !tiles_run.empty());
+    if (want_ws) {
+        auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
+        const int rec = tg::state_record_bytes(s->prec), ent = tg::entry_record_bytes(s->prec);
+        int64_t mS = 0, mE = 0, mH = 0;
+        for (const tg::TileInfo &ti : tiles_run) {
+            mS = std::max<int64_t>(mS, ti.nm + ti.nh);
+            mE = std::max<int64_t>(mE, ti.ne);
+            mH = std::max<int64_t>(mH, ti.nheavy);
+        }
+        int64_t mNh = 0, mA = 0, mI = 0;
+        for (const tg::TileInfo &ti : tiles_run) {
+            mNh = std::max<int64_t>(mNh, ti.nh);
+            mA = std::max<int64_t>(mA, ti.nact);
+            mI = std::max<int64_t>(mI, ti.inc_words);
+        }
+        tg::WsLayout &W = a.ws;
+        W.slots = (int32_t)al(mS * rec, 16);
+        W.act = (int32_t)al(W.slots + mE * ent, 16);
+        W.inc = (int32_t)al(W.act + mA * ent, 16);
+        W.stage = (int32_t)al(W.inc + mI * 2, 128);
+        W.idx_words = (int32_t)al(mNh, 4);
+        W.heavy_cap = (int32_t)std::max<int64_t>(1, mH);
+        const int64_t tail = 2 * (int64_t)W.idx_words * 4 + al(2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16) +
+                             (2 * tg::kWsMaxStages + 2) * 8 + 32;
+        const int64_t room = 227 * 1024 - tail;
+        W.nstages = (int32_t)std::min<int64_t>(tg::kWsMaxStages, room / std::max<int64_t>(1, W.stage));
+        if (W.nstages < 2 && s->kernel_req == 4)
+            return s->fail(TITAN_GB300_ELIMIT, "two tiles do not fit in shared memory for the warp-specialised kernel");
+    }
+    if (want_ws && a.ws.nstages >= 2) {
+        auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
+        tg::WsLayout &W = a.ws;
+        W.idx = W.nstages * W.stage;
+        W.heavy = W.idx + 2 * W.idx_words * 4;
+        W.mbar = (int32_t)al(W.heavy + 2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16);
+        W.total = W.mbar + (2 * W.nstages + 2) * 8 + 32;
+        s->ws_warps = s->threads_req > 0 ? s->threads_req / 32 : tg::kWsMaxConsumerWarps;
+        s->ws_warps = std::max(2, std::min(tg::kWsMaxConsumerWarps, s->ws_warps)) & ~1;
+        CK(tg::step_ws_prepare(s->prec, (size_t)W.total), "set shared memory");
+        int sms = 0, dev = 0;
+        CK(cudaGetDevice(&dev), "device");
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
+        s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), sms);
+        s->threads = (s->ws_warps + 1) * 32;
+        s->use_ws = true;
+    }
     s->use_pipe = s->kernel_req == 2 && a.pipe.total <= 227 * 1024;
     if (s->kernel_req == 2 && !s->use_pipe)
         return s->fail(TITAN_GB300_ELIMIT, "tiles too large for the pipelined kernel's two shared-memory stages");
@@ -499,9 +564,19 @@ int build_device(titan_gb300_sim *s) {
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
         per_sm = std::max(1, (227 * 1024) / a.pipe.total);
         s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), (int64_t)sms * per_sm);
-    } else {
+    } else if (!s->use_ws) {
         if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
-        CK(tg::step_prepare(s->prec, s->smem), "set shared memory");
+        s->use_async = s->kernel_req == 3;
+        s->step_variant = 0;
+        if (s->min_ctas_req >= 3 && s->prec != P_FP64) {
+            if (s->threads > 256)
+                return s->fail(TITAN_GB300_EINVAL, "3 or 4 CTAs per SM need at most 256 threads per CTA");
+            s->step_variant = s->min_ctas_req == 3 ? 1 : 2;
+        }
+        if (s->use_async)
+            CK(tg::step_async_prepare(s->prec, s->smem), "set shared memory");
+        else
+            CK(tg::step_prepare(s->prec, s->step_variant, s->smem), "set shared memory");
     }
     a.ntiles = (int32_t)tiles_run.size();
     if (P.ent_ends.size() > (size_t)INT32_MAX || P.halo.size() > (size_t)INT32_MAX)
@@ -717,9 +792,18 @@ int titan_gb300_set_launch(titan_gb300_sim *s, int threads_per_cta) {
     return TITAN_GB300_OK;
 }
 
+int titan_gb300_set_occupancy(titan_gb300_sim *s, int min_ctas_per_sm) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (min_ctas_per_sm < 0 || min_ctas_per_sm > 4 || min_ctas_per_sm == 2)
+        return s->fail(TITAN_GB300_EINVAL, "minimum CTAs per SM must be 0, 1, 3 or 4");
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "set the occupancy before start");
+    s->min_ctas_req = min_ctas_per_sm;
+    return TITAN_GB300_OK;
+}
+
 int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
     if (!s) return TITAN_GB300_EINVAL;
-    if (variant < 0 || variant > 2) return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0, 1 or 2");
+    if (variant < 0 || variant > 4) return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0 to 4");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "choose the kernel before start");
     s->kernel_req = variant;
     return TITAN_GB300_OK;
@@ -727,10 +811,10 @@ int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
 
 int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
     if (!s || !out) return TITAN_GB300_EINVAL;
-    out[0] = s->use_pipe ? 2 : 1;
-    out[1] = s->use_pipe ? s->ctas : s->args.ntiles;
+    out[0] = s->use_pipe ? 2 : (s->use_async ? 3 : (s->use_ws ? 4 : 1));
+    out[1] = (s->use_pipe || s->use_ws) ? s->ctas : s->args.ntiles;
     out[2] = s->threads;
-    out[3] = s->use_pipe ? s->args.pipe.total : (int64_t)s->smem;
+    out[3] = s->use_pipe ? s->args.pipe.total : (s->use_ws ? s->args.ws.total : (int64_t)s->smem);
     return TITAN_GB300_OK;
 }
 

@@ -44,6 +44,19 @@ struct PipeLayout {
 };
 constexpr int kPipeTileCache = 64;
 
+// Shared-memory layout of the warp-specialised persistent kernel
+// (step_ws.cu): nstages stages, each [state records | slab records / force
+// slots | actuation records | incidence block], the two-entry halo-index
+// ring, the heavy-mass sums, then 2 * nstages + 2 mbarriers and the control
+// words.
+struct WsLayout {
+    int32_t slots, act, inc, stage, nstages;  // offsets inside a stage, stage size
+    int32_t idx, idx_words;                   // halo-index ring (2 entries of idx_words int32)
+    int32_t heavy, heavy_cap, mbar, total;    // heavy sums: 2 groups x 3 x heavy_cap
+};
+constexpr int kWsMaxStages = 3;
+constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
+
 struct DevParams {
     double dt;
     double g[3];
@@ -87,6 +100,7 @@ struct StepArgs {
     int32_t ntiles;
     int *err;                  // set by a kernel whose bounded wait gave up
     PipeLayout pipe;
+    WsLayout ws;
 };
 
 // Body-resident batched launch (resident.cu, plan.h ResPlan): bins of whole
@@ -140,14 +154,32 @@ constexpr int kDiagQ = 9;
 int state_words(int precision);
 // dynamic shared memory of one tile's CTA
 size_t tile_smem_bytes(int precision, int slots, int entries, int heavy);
-cudaError_t step_prepare(int precision, size_t smem);
-cudaError_t launch_step(int precision, const StepArgs &a, int ntiles, int threads, size_t smem,
+// Per-tile kernel, launch-bound variant 0: (512 threads, 1 CTA/SM), every
+// precision; FP32 forms also 1: (256, 3) and 2: (256, 4) -- at most 256
+// threads per CTA, registers capped for 3 or 4 resident CTAs per SM.
+constexpr int kStepVariants = 3;
+const void *step_kernel_capped(int precision, int variant);  // null if not compiled
+cudaError_t step_prepare(int precision, int variant, size_t smem);
+cudaError_t launch_step(int precision, int variant, const StepArgs &a, int ntiles, int threads, size_t smem,
                         int parity, int write_acc, cudaStream_t s);
 // Pipelined persistent variant (step_tma.cu): grid of `ctas` CTAs walking the
 // tiles, TMA bulk copies of the next tile overlapping the current tile.
 cudaError_t step_pipe_prepare(int precision, size_t smem);
 cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int threads, int parity, int write_acc,
                              cudaStream_t s);
+// Per-tile kernel with asynchronous staging (step_async.cu): slab records and
+// tile states by bulk copy, halo by cp.async, one wait.  Shared memory per
+// CTA: tile_async_smem_bytes.
+size_t tile_async_smem_bytes(int precision, int slots, int entries, int heavy);
+cudaError_t step_async_prepare(int precision, size_t smem);
+cudaError_t launch_step_async(int precision, const StepArgs &a, int ntiles, int threads, size_t smem, int parity,
+                              int write_acc, cudaStream_t s);
+// Warp-specialised persistent kernel (step_ws.cu): `ctas` CTAs of
+// consumer_warps + 1 warps; the last warp streams tiles into a ring of
+// stages, the others compute.
+cudaError_t step_ws_prepare(int precision, size_t smem);
+cudaError_t launch_step_ws(int precision, const StepArgs &a, int ctas, int consumer_warps, int parity,
+                           int write_acc, cudaStream_t s);
 // bytes of one state record / one slab entry record for a precision
 int state_record_bytes(int precision);
 int entry_record_bytes(int precision);

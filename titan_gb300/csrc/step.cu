@@ -1,184 +1,11 @@
-// step.cu -- fused mass-spring step for sm_103a, per-tile form.
-//
-// One CTA per tile (plan.h).  Per step and tile:
-//   A. stage the state records of the tile's masses and of its halo in
-//      shared memory (16-byte vector copies, two records in flight per
-//      thread);
-//   B. compute every slab entry's spring force once (src/sim.cu:1054-1065)
-//      into its shared-memory force slot (tile_phases.cuh);
-//   C. per mass, sum its incident slots in ascending spring order (one legal
-//      serialisation of the reference's atomics, src/vec.cu:33-37), then
-//      the per-mass epilogue (epilogue.cuh: src/sim.cu:1100-1166) writes the
-//      other ping-pong buffer.
-// A thread's own mass's phase-C inputs (flags, degree, m, incidence words)
-// are fetched before phase A so that their latency hides behind A and B.
-// Kernels are compiled without FMA contraction (build flag --fmad=false):
-// the FP64 form then rounds each operation as the CPU oracle does.
+// step.cu -- host side of the per-tile step kernel (step_kernel.cuh): the
+// FP64 form and the default launch bounds of every precision; the
+// register-capped variants of the FP32 forms are in step_var.cu.
 #include <cstdint>
 
-#include "engine.h"
-#include "epilogue.cuh"
-#include "state.cuh"
-#include "step_math.cuh"
-#include "tile_phases.cuh"
+#include "step_kernel.cuh"
 
 namespace tg {
-
-namespace {
-
-constexpr int kBatchC = 4;     // 8-byte incidence words in flight per thread (phase C)
-constexpr int kPrefetchW = 7;  // incidence words (28 codes) fetched before phase B
-
-// slab entries in flight per thread in phase B (FP64 records are 32 B)
-template <int PREC>
-__host__ __device__ constexpr int batch_b() { return PREC == P_FP64 ? 2 : 4; }
-
-template <int PREC>
-__host__ __device__ constexpr int rec_bytes() { return PREC == P_FP32 ? 32 : 48; }
-
-__host__ __device__ constexpr int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
-
-template <int PREC>
-__device__ __forceinline__ void copy_record(uint8_t *dst, const uint8_t *src) {
-    constexpr int kV = rec_bytes<PREC>() / 16;
-#pragma unroll
-    for (int v = 0; v < kV; v++)
-        reinterpret_cast<float4 *>(dst)[v] = __ldg(reinterpret_cast<const float4 *>(src) + v);
-}
-
-template <int PREC>
-__global__ void __launch_bounds__(512) k_step(StepArgs a, int parity, int write_acc) {
-    using R = typename Real<PREC>::T;
-    constexpr int kRec = rec_bytes<PREC>();
-    constexpr int kSlot = Slot<PREC>::kBytes;
-    extern __shared__ __align__(16) uint8_t smem[];
-    const TileInfo ti = a.tiles[blockIdx.x];
-    const int S = ti.nm + ti.nh, E = ti.ne;
-    uint8_t *st = smem;                                   // S state records
-    uint8_t *slots = smem + align16((int64_t)S * kRec);   // E force slots
-    R *sH = reinterpret_cast<R *>(slots + (int64_t)E * kSlot);  // 3 * nheavy
-    const uint8_t *in = reinterpret_cast<const uint8_t *>(parity ? a.state1 : a.state0);
-    void *out = parity ? a.state0 : a.state1;
-    const int64_t np = a.npad;
-    const DevParams *prm = a.prm;
-    const StepTime t = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->dt;
-
-    // phase-C inputs of this thread's own mass, issued first
-    const int i_own = threadIdx.x;
-    uint8_t fl_own = MF_FIXED;
-    uint32_t d_own = 0, woff_own = 0;
-    R m_own = 1;
-    uint2 cw_own[kPrefetchW];
-    if (i_own < ti.nm) {
-        const int64_t g = (int64_t)ti.mass_off + i_own;
-        fl_own = __ldg(a.flags + g);
-        d_own = __ldg(a.deg + g);
-        m_own = __ldg(reinterpret_cast<const R *>(a.mass) + g);
-        woff_own = __ldg(a.warp_inc_off + ti.warp_off + (i_own >> 5));
-    }
-
-    // ---- A: stage tile + halo records, two in flight per thread ---------
-    for (int i0 = threadIdx.x; i0 < S; i0 += 2 * blockDim.x) {
-        const int i1 = i0 + blockDim.x;
-        const int64_t g0 = i0 < ti.nm ? (int64_t)ti.mass_off + i0 : (int64_t)__ldg(a.halo + ti.halo_off + i0 - ti.nm);
-        int64_t g1 = g0;
-        if (i1 < S) g1 = i1 < ti.nm ? (int64_t)ti.mass_off + i1 : (int64_t)__ldg(a.halo + ti.halo_off + i1 - ti.nm);
-        float4 v0[kRec / 16], v1[kRec / 16];
-#pragma unroll
-        for (int v = 0; v < kRec / 16; v++) v0[v] = __ldg(reinterpret_cast<const float4 *>(in + g0 * kRec) + v);
-        if (i1 < S) {
-#pragma unroll
-            for (int v = 0; v < kRec / 16; v++) v1[v] = __ldg(reinterpret_cast<const float4 *>(in + g1 * kRec) + v);
-        }
-#pragma unroll
-        for (int v = 0; v < kRec / 16; v++) reinterpret_cast<float4 *>(st + (int64_t)i0 * kRec)[v] = v0[v];
-        if (i1 < S) {
-#pragma unroll
-            for (int v = 0; v < kRec / 16; v++) reinterpret_cast<float4 *>(st + (int64_t)i1 * kRec)[v] = v1[v];
-        }
-    }
-    // the first incidence words of this thread's mass
-    if (i_own < ti.nm && d_own != 255) {
-        const uint2 *ip = reinterpret_cast<const uint2 *>(a.inc + woff_own) + (i_own & 31);
-        const uint32_t nw = (d_own + 3) >> 2;
-#pragma unroll
-        for (int w = 0; w < kPrefetchW; w++)
-            if ((uint32_t)w < nw) cw_own[w] = __ldg(ip + 32 * w);
-    }
-    __syncthreads();
-
-    // ---- B: one force per slab entry (kBatchB records in flight) ----------
-    {
-        const uint8_t *ent = reinterpret_cast<const uint8_t *>(a.ent) + (int64_t)ti.ent_off * kSlot;
-        const uint8_t *act = reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * kSlot;
-        constexpr int kBatchB = batch_b<PREC>();
-        for (int e0 = threadIdx.x; e0 < E; e0 += kBatchB * blockDim.x) {
-            Rec16<PREC> r[kBatchB], q[kBatchB];
-#pragma unroll
-            for (int k = 0; k < kBatchB; k++) {
-                const int e = e0 + k * blockDim.x;
-                if (e < E) r[k] = ldg_rec<PREC>(ent + (int64_t)e * kSlot);
-                if (e < ti.nact) q[k] = ldg_rec<PREC>(act + (int64_t)e * kSlot);
-            }
-#pragma unroll
-            for (int k = 0; k < kBatchB; k++) {
-                const int e = e0 + k * blockDim.x;
-                if (e >= E) break;
-                entry_force<PREC>(r[k], e < ti.nact, q[k], st, t, slots + (int64_t)e * kSlot);
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- C0: heavy masses --------------------------------------------------
-    if (ti.nheavy > 0) {
-        heavy_sums<PREC>(a, ti, slots, sH);
-        __syncthreads();
-    }
-
-    // ---- C: per-mass gather, constraints, integration ----------------------
-    for (int i = threadIdx.x; i < ti.nm; i += blockDim.x) {
-        const int64_t g = (int64_t)ti.mass_off + i;
-        const bool own = i == i_own;
-        const uint8_t fl = own ? fl_own : __ldg(a.flags + g);
-        if (fl & MF_FIXED) continue;  // src/sim.cu:1100
-        const uint32_t d = own ? d_own : __ldg(a.deg + g);
-        const R m = own ? m_own : __ldg(reinterpret_cast<const R *>(a.mass) + g);
-        R F0 = 0, F1 = 0, F2 = 0;
-        if (d == 255) {
-            int h = 0;
-            while (h < ti.nheavy && a.heavy_local[ti.heavy_off + h] != i) h++;
-            F0 = F0 + sH[h];
-            F1 = F1 + sH[ti.nheavy + h];
-            F2 = F2 + sH[2 * ti.nheavy + h];
-        } else if (d > 0) {
-            const uint32_t woff = own ? woff_own : __ldg(a.warp_inc_off + ti.warp_off + (i >> 5));
-            const uint2 *ip = reinterpret_cast<const uint2 *>(a.inc + woff) + (i & 31);
-            const uint32_t nw = (d + 3) >> 2;
-            uint32_t w0 = 0;
-            if (own) {
-#pragma unroll
-                for (int w = 0; w < kPrefetchW; w++)
-                    if ((uint32_t)w < nw) gather_word<PREC>(slots, cw_own[w], w, d, F0, F1, F2);
-                w0 = kPrefetchW;
-            }
-            for (; w0 < nw; w0 += kBatchC) {
-                uint2 cw[kBatchC];
-#pragma unroll
-                for (int k = 0; k < kBatchC; k++)
-                    if (w0 + k < nw) cw[k] = __ldg(ip + 32 * (w0 + k));
-#pragma unroll
-                for (int k = 0; k < kBatchC; k++)
-                    if (w0 + k < nw) gather_word<PREC>(slots, cw[k], w0 + k, d, F0, F1, F2);
-            }
-        }
-        St<PREC> s = load_state_smem<PREC>(st, i);
-        integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, s, out, g, write_acc, np, prm);
-    }
-}
-
-}  // namespace
 
 int state_words(int precision) { return precision == P_FP64 ? 6 : (precision == P_FP32C ? 12 : 8); }
 
@@ -189,22 +16,26 @@ size_t tile_smem_bytes(int precision, int slots, int entries, int heavy) {
     return (size_t)(align16((int64_t)slots * rec) + (int64_t)entries * slot + 3 * (int64_t)heavy * rs);
 }
 
-cudaError_t step_prepare(int precision, size_t smem) {
-    const void *f = precision == P_FP64   ? (const void *)k_step<P_FP64>
-                    : precision == P_FP32 ? (const void *)k_step<P_FP32>
-                                          : (const void *)k_step<P_FP32C>;
+const void *step_kernel(int precision, int variant) {
+    if (variant != 0 && precision != P_FP64) return step_kernel_capped(precision, variant);
+    return precision == P_FP64   ? (const void *)k_step<P_FP64, 512, 1>
+           : precision == P_FP32 ? (const void *)k_step<P_FP32, 512, 1>
+                                 : (const void *)k_step<P_FP32C, 512, 1>;
+}
+
+cudaError_t step_prepare(int precision, int variant, size_t smem) {
+    const void *f = step_kernel(precision, variant);
+    if (!f) return cudaErrorInvalidValue;
     return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-cudaError_t launch_step(int precision, const StepArgs &a, int ntiles, int threads, size_t smem,
+cudaError_t launch_step(int precision, int variant, const StepArgs &a, int ntiles, int threads, size_t smem,
                         int parity, int write_acc, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    switch (precision) {
-        case P_FP64: k_step<P_FP64><<<ntiles, threads, smem, s>>>(a, parity, write_acc); break;
-        case P_FP32: k_step<P_FP32><<<ntiles, threads, smem, s>>>(a, parity, write_acc); break;
-        default: k_step<P_FP32C><<<ntiles, threads, smem, s>>>(a, parity, write_acc); break;
-    }
-    return cudaGetLastError();
+    const void *f = step_kernel(precision, variant);
+    if (!f) return cudaErrorInvalidValue;
+    void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
+    return cudaLaunchKernel(f, dim3(ntiles), dim3(threads), args, smem, s);
 }
 
 }  // namespace tg

@@ -17,6 +17,7 @@
 // its own copies (bounded) and returns; the host reports the error.
 #include <cstdint>
 
+#include "async_copy.cuh"
 #include "engine.h"
 #include "epilogue.cuh"
 #include "state.cuh"
@@ -27,59 +28,11 @@ namespace tg {
 
 namespace {
 
-constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before giving up
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// 1-D bulk copy global -> shared, completion counted on bar (bytes % 16 == 0,
-// both addresses 16-byte aligned)
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(__cvta_generic_to_global(src))
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 template <int PREC>
 struct Geo {
     static constexpr int kRec = PREC == P_FP32 ? 32 : 48;  // state record bytes
     static constexpr int kEnt = PREC == P_FP64 ? 32 : 16;  // slab / actuation record bytes
 };
-
-// Issues one tile's bulk copies into a stage; returns the byte count.
-__device__ __forceinline__ uint32_t issue_chunks(uint8_t *dst, const uint8_t *src, uint32_t bytes, uint64_t *bar) {
-    constexpr uint32_t kChunk = 32768;
-    for (uint32_t o = 0; o < bytes; o += kChunk) {
-        uint32_t b = bytes - o < kChunk ? bytes - o : kChunk;
-        bulk_g2s(dst + o, src + o, b, bar);
-    }
-    return bytes;
-}
 
 template <int PREC>
 __device__ __forceinline__ void issue_tile(const StepArgs &a, const TileInfo &ti, const void *in, uint8_t *stage,
@@ -248,7 +201,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
 
         // ---- C0: heavy masses (warp-cooperative, fixed order) --------------
         if (ti.nheavy > 0) {
-            heavy_sums<PREC>(a, ti, recb, sH);
+            heavy_sums<PREC>(a, ti, recb, sH, threadIdx.x >> 5, blockDim.x >> 5);
             __syncthreads();
         }
 

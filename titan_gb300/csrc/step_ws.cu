@@ -1,0 +1,321 @@
+// step_ws.cu -- warp-specialised persistent form of the fused step (sm_103a).
+//
+// Same tiles, arithmetic, summation order and results as k_step
+// (step_kernel.cuh) -- the tests check them bit for bit.  The per-tile forms
+// alternate, inside each CTA, between waiting for a tile's data and
+// computing on it; here the two run concurrently in one persistent CTA per
+// SM:
+//   * the producer warp walks the CTA's tiles (b, b + G, b + 2G, ...) and,
+//     for each, waits until a stage of the shared-memory ring is free, then
+//     streams the tile into it: the slab records (into the force slots) and
+//     the tile masses' state records as bulk copies on the Tensor Memory
+//     Accelerator, and the halo state records as 16-byte cp.async gathers by
+//     the warp's 32 lanes, all counted on the stage's "full" mbarrier (one
+//     expect-tx arrival plus one cp.async arrival per lane).  The halo index
+//     list of the next tile arrives by bulk copy into a two-entry ring while
+//     the current tile is issued, so no gather waits on an index load;
+//     The stage also receives the tile's actuation records and incidence
+//     block, so consumers never wait on a global load for them;
+//   * the consumer warps form two groups that take alternate tiles (while one
+//     group is in its narrow per-mass phase, the other computes entry
+//     forces).  A group waits for "full", computes each entry's force over
+//     its record (phase B), sums each mass's incident slots in ascending
+//     spring order and integrates (phase C), then releases the stage on its
+//     "empty" mbarrier.
+// Each group synchronises on its own named barrier (1 or 2).  Every wait is
+// bounded; a time-out is made uniform within a group (bar.red.or), raises
+// *err and the shared abort word, and the CTA drains its own copies
+// (bounded) before it returns.
+#include <cstdint>
+
+#include "async_copy.cuh"
+#include "engine.h"
+#include "epilogue.cuh"
+#include "state.cuh"
+#include "step_math.cuh"
+#include "tile_phases.cuh"
+
+namespace tg {
+
+namespace {
+
+constexpr int kBatchB = 2;  // slab entries per thread in flight (phase B)
+constexpr int kWsThreads = (kWsMaxConsumerWarps + 1) * 32;
+
+template <int PREC>
+__host__ __device__ constexpr int ws_rec() { return PREC == P_FP32 ? 32 : 48; }
+
+// Arrives on bar once this thread's earlier cp.async copies have landed
+// (the barrier's expected count includes this arrival).
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+// Named-barrier OR over a consumer group.
+__device__ __forceinline__ bool group_any(int id, int nthreads, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
+
+// Bounded wait; gives up early when another warp raised the abort word.
+__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word) {
+    for (uint32_t it = 0; it < kWaitLimit; it++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *abort_word) return false;
+    }
+    return false;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parity, int write_acc) {
+    using R = typename Real<PREC>::T;
+    constexpr int kRec = ws_rec<PREC>();
+    constexpr int kSlot = Slot<PREC>::kBytes;
+    extern __shared__ __align__(128) uint8_t smem[];
+    const WsLayout &L = a.ws;
+    const int NS = L.nstages;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + L.mbar);
+    uint64_t *empty = full + NS;
+    uint64_t *idxbar = empty + NS;  // [2]
+    volatile int *abort_word = reinterpret_cast<volatile int *>(idxbar + 2);
+    int *issued_word = reinterpret_cast<int *>(idxbar + 2) + 1;  // tiles whose copies were issued
+    int *idx_issued = issued_word + 1, *idx_waited = issued_word + 2;
+    int *last_word = issued_word + 3;                              // [2]: last tile each group consumed
+    int32_t *idxbuf = reinterpret_cast<int32_t *>(smem + L.idx);  // 2 * L.idx_words
+    const uint8_t *in = reinterpret_cast<const uint8_t *>(parity ? a.state1 : a.state0);
+    void *out = parity ? a.state0 : a.state1;
+    const int64_t np = a.npad;
+    const DevParams *prm = a.prm;
+    const StepTime tm = step_time(a.tbuf[parity]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + prm->dt;
+    const int ncw = (int)(blockDim.x >> 5) - 1;  // consumer warps (even)
+    const int gw = ncw >> 1;                     // warps per group
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int G = gridDim.x;
+    const int ntiles = a.ntiles;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; s++) {
+            mbar_init(&full[s], 33);  // expect-tx arrival + one cp.async arrival per producer lane
+            mbar_init(&empty[s], (uint32_t)gw);
+        }
+        mbar_init(&idxbar[0], 1);
+        mbar_init(&idxbar[1], 1);
+        *abort_word = 0;
+        *issued_word = 0;
+        *idx_issued = 0;
+        *idx_waited = 0;
+        last_word[0] = last_word[1] = -1;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    if (warp == ncw) {
+        // ---------------- producer warp ----------------
+        constexpr int kChunks = kRec / 16;
+        // halo indices of tile j go to ring entry j & 1 (lists are padded to
+        // a multiple of 4 entries, so each copy is a multiple of 16 bytes)
+        auto issue_idx = [&](int j, const TileInfo &tj) {
+            const uint32_t b = (uint32_t)((tj.nh + 3) & ~3) * 4u;
+            fence_proxy_async();
+            mbar_expect_tx(&idxbar[j & 1], b);
+            issue_chunks(reinterpret_cast<uint8_t *>(idxbuf + (j & 1) * L.idx_words),
+                         reinterpret_cast<const uint8_t *>(a.halo + tj.halo_off), b, &idxbar[j & 1]);
+            *idx_issued = j + 1;
+        };
+        TileInfo ti = {};
+        if (blockIdx.x < ntiles) ti = a.tiles[blockIdx.x];
+        if (lane == 0 && blockIdx.x < ntiles) issue_idx(0, ti);
+        int k = 0;
+        for (int t = blockIdx.x; t < ntiles; t += G, k++) {
+            const int s = k % NS;
+            const uint32_t ph = (uint32_t)(k / NS) & 1u;
+            const bool has_next = t + G < ntiles;
+            TileInfo tn = {};
+            if (has_next) tn = a.tiles[t + G];
+            bool ok = ws_wait(&empty[s], ph ^ 1u, abort_word);
+            if (ok) {
+                ok = ws_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
+                if (ok && lane == 0) *idx_waited = k + 1;
+            }
+            if (__any_sync(0xffffffffu, !ok)) {
+                if (lane == 0) {
+                    *abort_word = 1;
+                    atomicOr(a.err, 1);
+                }
+                break;
+            }
+            uint8_t *st = smem + (int64_t)s * L.stage;
+            if (lane == 0) {
+                fence_proxy_async();
+                const uint32_t eb = (uint32_t)ti.ne * kSlot, ab = (uint32_t)ti.nact * kSlot;
+                const uint32_t ib = (uint32_t)ti.inc_words * 2u, sb = (uint32_t)ti.nm * kRec;
+                mbar_expect_tx(&full[s], eb + ab + ib + sb);
+                issue_chunks(st + L.slots, reinterpret_cast<const uint8_t *>(a.ent) + (int64_t)ti.ent_off * kSlot,
+                             eb, &full[s]);
+                issue_chunks(st + L.act, reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * kSlot, ab,
+                             &full[s]);
+                issue_chunks(st + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), ib, &full[s]);
+                issue_chunks(st, in + (int64_t)ti.mass_off * kRec, sb, &full[s]);
+            }
+            const int32_t *ix = idxbuf + (k & 1) * L.idx_words;
+            for (int q = lane; q < ti.nh * kChunks; q += 32) {
+                const int h = q / kChunks, c = q - h * kChunks;
+                cp_async16(st + (int64_t)(ti.nm + h) * kRec + 16 * c, in + (int64_t)ix[h] * kRec + 16 * c);
+            }
+            cp_async_arrive(&full[s]);
+            __syncwarp();  // every lane has read ring entry k & 1
+            if (lane == 0) {
+                *issued_word = k + 1;
+                if (has_next) issue_idx(k + 1, tn);
+            }
+            ti = tn;
+        }
+    } else {
+        // ---------------- consumer groups ----------------
+        const int grp = warp / gw;
+        const int gt = threadIdx.x - grp * gw * 32;  // thread index within the group
+        const int gn = gw * 32;
+        const int bar_id = 1 + grp;
+        R *sH = reinterpret_cast<R *>(smem + L.heavy) + grp * 3 * L.heavy_cap;
+        for (int k = grp, t = blockIdx.x + grp * G; t < ntiles; k += 2, t += 2 * G) {
+            const int s = k % NS;
+            const uint32_t ph = (uint32_t)(k / NS) & 1u;
+            const TileInfo ti = a.tiles[t];
+            const int E = ti.ne;
+            // per-mass scalars of this group's first masses, loaded while the copies land
+            const int i_own = gt;
+            uint8_t fl_own = MF_FIXED;
+            uint32_t d_own = 0, woff_own = 0;
+            R m_own = 1;
+            if (i_own < ti.nm) {
+                const int64_t g = (int64_t)ti.mass_off + i_own;
+                fl_own = __ldg(a.flags + g);
+                d_own = __ldg(a.deg + g);
+                m_own = __ldg(reinterpret_cast<const R *>(a.mass) + g);
+                woff_own = __ldg(a.warp_inc_off + ti.warp_off + (i_own >> 5));
+            }
+            const bool ok = ws_wait(&full[s], ph, abort_word);
+            if (group_any(bar_id, gn, !ok)) {
+                if (gt == 0) {
+                    *abort_word = 1;
+                    atomicOr(a.err, 1);
+                }
+                break;
+            }
+            if (gt == 0) last_word[grp] = k;
+            uint8_t *st = smem + (int64_t)s * L.stage;
+            uint8_t *slots = st + L.slots;
+            const uint8_t *actb = st + L.act;
+            const uint16_t *incs = reinterpret_cast<const uint16_t *>(st + L.inc);
+
+            // ---- B: one force per slab entry, written over its record ----
+            for (int e0 = gt; e0 < E; e0 += kBatchB * gn) {
+                Rec16<PREC> r[kBatchB], q[kBatchB];
+#pragma unroll
+                for (int j = 0; j < kBatchB; j++) {
+                    const int e = e0 + j * gn;
+                    if (e < E) r[j] = load_rec<PREC>(slots + (int64_t)e * kSlot);
+                    if (e < ti.nact) q[j] = load_rec<PREC>(actb + (int64_t)e * kSlot);
+                }
+#pragma unroll
+                for (int j = 0; j < kBatchB; j++) {
+                    const int e = e0 + j * gn;
+                    if (e < E) entry_force<PREC>(r[j], e < ti.nact, q[j], st, tm, slots + (int64_t)e * kSlot);
+                }
+            }
+            group_sync(bar_id, gn);
+
+            // ---- C0: heavy masses ----
+            if (ti.nheavy > 0) {
+                heavy_sums<PREC>(a, ti, slots, sH, warp - grp * gw, gw);
+                group_sync(bar_id, gn);
+            }
+
+            // ---- C: per-mass gather, constraints, integration ----
+            for (int i = gt; i < ti.nm; i += gn) {
+                const int64_t g = (int64_t)ti.mass_off + i;
+                const bool own = i == i_own;
+                const uint8_t fl = own ? fl_own : __ldg(a.flags + g);
+                if (fl & MF_FIXED) continue;  // src/sim.cu:1100
+                const uint32_t d = own ? d_own : __ldg(a.deg + g);
+                const R m = own ? m_own : __ldg(reinterpret_cast<const R *>(a.mass) + g);
+                R F0 = 0, F1 = 0, F2 = 0;
+                if (d == 255) {
+                    int h = 0;
+                    while (h < ti.nheavy && a.heavy_local[ti.heavy_off + h] != i) h++;
+                    F0 = F0 + sH[h];
+                    F1 = F1 + sH[ti.nheavy + h];
+                    F2 = F2 + sH[2 * ti.nheavy + h];
+                } else if (d > 0) {
+                    const uint32_t woff =
+                        (own ? woff_own : __ldg(a.warp_inc_off + ti.warp_off + (i >> 5))) - (uint32_t)ti.inc_off;
+                    const uint2 *ip = reinterpret_cast<const uint2 *>(incs + woff) + (i & 31);
+                    const uint32_t nw = (d + 3) >> 2;
+                    for (uint32_t w = 0; w < nw; w++) gather_word<PREC>(slots, ip[32 * w], w, d, F0, F1, F2);
+                }
+                St<PREC> sv = load_state_smem<PREC>(st, i);
+                integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, sv, out, g, write_acc, np, prm);
+            }
+            // the stage is free once every warp of the group is past it; order
+            // this thread's slot writes before the copies that will reuse it
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]);
+        }
+    }
+
+    // drain: copies issued for tiles nobody consumed and index lists nobody
+    // waited for (only after an abort)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int issued = *issued_word;
+        for (int k = 0; k < issued; k++) {
+            if (k <= last_word[k & 1]) continue;
+            const int s = k % NS;
+            const uint32_t ph = (uint32_t)(k / NS) & 1u;
+            for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&full[s], ph); it++) {
+            }
+        }
+        for (int j = *idx_waited; j < *idx_issued; j++)
+            for (uint32_t it = 0; it < kWaitLimit && !mbar_try_wait(&idxbar[j & 1], (uint32_t)(j >> 1) & 1u); it++) {
+            }
+    }
+}
+
+template <int PREC>
+const void *ws_kernel() {
+    return (const void *)k_step_ws<PREC>;
+}
+
+const void *ws_kernel(int precision) {
+    return precision == P_FP64 ? ws_kernel<P_FP64>() : precision == P_FP32 ? ws_kernel<P_FP32>() : ws_kernel<P_FP32C>();
+}
+
+}  // namespace
+
+cudaError_t step_ws_prepare(int precision, size_t smem) {
+    return cudaFuncSetAttribute(ws_kernel(precision), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_step_ws(int precision, const StepArgs &a, int ctas, int consumer_warps, int parity,
+                           int write_acc, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    if (consumer_warps < 2 || consumer_warps > kWsMaxConsumerWarps || (consumer_warps & 1))
+        return cudaErrorInvalidValue;
+    void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
+    return cudaLaunchKernel(ws_kernel(precision), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
+                            (size_t)a.ws.total, s);
+}
+
+}  // namespace tg

@@ -75,6 +75,21 @@ __device__ __forceinline__ Rec16<PREC> ldg_rec(const uint8_t *p) {  // read-only
     return r;
 }
 
+// The same from a stream read once per step (slab entries, actuation
+// records): evict-first in L1 and L2 (ld.global.cs), so that the state
+// records, re-read by neighbouring tiles and by the next step, keep L2.
+template <int PREC>
+__device__ __forceinline__ Rec16<PREC> ldcs_rec(const uint8_t *p) {
+    Rec16<PREC> r;
+    if constexpr (PREC == P_FP64) {
+        r.lo = __ldcs(reinterpret_cast<const double2 *>(p));
+        r.hi = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+    } else {
+        r.v = __ldcs(reinterpret_cast<const float4 *>(p));
+    }
+    return r;
+}
+
 template <int PREC>
 struct F3 {
     typename Real<PREC>::T x, y, z;
@@ -200,11 +215,12 @@ __device__ __forceinline__ void gather_word(const uint8_t *slots, uint2 cw, uint
 
 // Warp-cooperative, fixed-order sum over a heavy mass's incidence list
 // (lane l takes codes l, l+32, ...; then an xor butterfly).
+// warp / nw: this warp's index among the nw warps sharing the work.
 template <int PREC>
 __device__ __forceinline__ void heavy_sums(const StepArgs &a, const TileInfo &ti, const uint8_t *slots,
-                                           typename Real<PREC>::T *sH) {
+                                           typename Real<PREC>::T *sH, int warp, int nw) {
     using R = typename Real<PREC>::T;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31;
     for (int h = warp; h < ti.nheavy; h += nw) {
         const int64_t gh = (int64_t)ti.heavy_off + h;
         const uint32_t q0 = a.heavy_inc_off[gh], q1 = a.heavy_inc_off[gh + 1];

@@ -153,7 +153,7 @@ def config3(nbodies=4096, seed=3, side_range=(3, 12), spacing=0.1, pitch=2.0):
     return sc
 
 
-def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0, resident=None):
+def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0, resident=None, occupancy=0):
     """Upload a scene into a Sim handle (and start it).  resident: None for
     the default, else (mode, bin_masses, threads) for set_resident."""
     sim.set_time_step(sc["dt"])
@@ -179,10 +179,13 @@ def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0, res
         sim.set_kernel(kernel)
     if resident is not None:
         sim.set_resident(*resident)
+    if occupancy:
+        sim.set_occupancy(occupancy)
     if start:
         sim.start(tile_masses)
     return sim
 
 
-def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0, kernel=0, resident=None) -> Sim:
-    return load(Sim(precision, device), sc, True, tile_masses, threads, kernel, resident)
+def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0, kernel=0, resident=None,
+             occupancy=0) -> Sim:
+    return load(Sim(precision, device), sc, True, tile_masses, threads, kernel, resident, occupancy)
