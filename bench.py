@@ -53,6 +53,12 @@ def parse():
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--threads", type=int, default=0)
     p.add_argument("--kernel", type=int, default=0, help="0 auto, 1 per-tile, 2 pipelined")
+    p.add_argument("--suite", action="store_true",
+                   help="instead of the headline line: one JSON line per workload of the baseline table "
+                        "(5^3, 100^3, 4096 bodies; engine FP64/FP32C, the reference's CUDA kernels, the CPU port)")
+    p.add_argument("--precision-study", action="store_true",
+                   help="instead of the headline line: 64^3 lattice at dt=1e-5, FP32 and FP32C against FP64")
+    p.add_argument("--study-steps", type=int, default=20000)
     p.add_argument("--ref-gpu-steps", type=int, default=50,
                    help="steps of the reference's own CUDA kernels timed beside ours (0: skip)")
     return p.parse_args()
@@ -292,7 +298,9 @@ def run_ours(a, rank, world, local):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
                      "implementation_bytes_per_launch": info["implementation_bytes_per_step"],
-                     "kernel": "k_step (fused spring forces + mass update, one launch per step)"},
+                     "kernel": {"warp-specialised": "k_step_ws", "per-tile": "k_step", "pipelined": "k_step_pipe",
+                                "per-tile-async": "k_step_async"}.get(kinfo["kernel"], kinfo["kernel"])
+                     + " (fused spring forces + mass update, one launch per step)"},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * nm * 8 / a.e2e_chunk,
                 "d2h_bytes_per_step": 3 * nm * 8 / a.e2e_chunk, "steps_per_call": a.e2e_chunk,
                 "calls": a.e2e_calls,
@@ -337,9 +345,132 @@ def run_reference(a, rank, world):
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def _event_ms(sim, steps, local):
+    import torch
+    stream = torch.cuda.ExternalStream(sim.stream, device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    sim.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_suite(a, local):
+    """Rows of the baseline table: each workload timed with the engine (FP64
+    and FP32C, automatic kernel), the reference's own CUDA kernels on the same
+    GPU (back to back and with execute()'s per-step synchronisation) and the
+    CPU port of the reference on all host cores.  Every value is
+    spring-updates/s over a bounded sample of the workload's steps."""
+    import torch
+
+    import titan_gb300 as tg
+    from oracle import pyoracle as po
+    from oracle import refgpu
+    from titan_gb300 import workloads as wl
+
+    torch.cuda.set_device(local)
+    threads = os.cpu_count() or 1
+    rows = [
+        ("5^3 lattice, contact + friction (config 1 contact variant)", wl.config1(contact=True), 10000, 2000,
+         5000, 2000),
+        ("100^3 lattice, 20% actuated, plane + ball (config 2)", wl.config2(), 1000, 200, 50, 4),
+        ("4096 bodies, 3-12 masses per side, own planes (config 3)", wl.config3(nbodies=4096), 5000, 200, 20, 4),
+    ]
+    for name, sc, steps, eng_steps, ref_steps, cpu_steps in rows:
+        ns, nm = sc["left"].size, sc["pos"].shape[0]
+        out = {"workload": name, "masses": nm, "springs": ns, "steps_of_workload": steps, "unit": UNIT}
+        for prec, key in ((tg.FP32C, "engine_f32c"), (tg.FP64, "engine_f64")):
+            sim = wl.make_sim(sc, prec, 0, device=local)
+            k = eng_steps if prec != tg.FP64 else max(1, eng_steps // 4)
+            sim.step(3)
+            ms = _event_ms(sim, k, local)
+            out[key] = {"value": ns * k / (ms / 1e3), "ms_per_step": ms / k, "steps_timed": k,
+                        "kernel": sim.kernel_info()["kernel"]}
+            sim.close()
+        why = refgpu.available()
+        if why:
+            out["reference_cuda_kernels"] = {"unavailable": why}
+        else:
+            rsc = dict(sc)
+            note = "reference src/sim.cu kernels, 1024-thread blocks, FP64 atomics"
+            if "body_ptr" in sc:  # the reference has no per-body planes: one global plane does the same work
+                rsc["planes"] = sc["planes"] + [((0.0, 0.0, 1.0), 0.0, 0.5, 0.5)]
+                note += "; per-body planes replaced by one global plane (same per-mass work)"
+            r = refgpu.RefGpuSim(rsc, local)
+            try:
+                r.step(3)
+                ms = r.time_steps(ref_steps)
+                ms_sync = r.time_steps(ref_steps, sync_each=True)
+            finally:
+                r.close()
+            out["reference_cuda_kernels"] = {"value": ns * ref_steps / (ms / 1e3), "ms_per_step": ms / ref_steps,
+                                             "ms_per_step_with_step_sync": ms_sync / ref_steps,
+                                             "steps_timed": ref_steps, "note": note}
+        o = po.OracleSim(sc)
+        t0 = time.perf_counter()
+        o.step(cpu_steps, po.ATOMIC_OMP, threads)
+        dt = time.perf_counter() - t0
+        out["reference_cpu_port"] = {"value": ns * cpu_steps / dt, "ms_per_step": dt / cpu_steps * 1e3,
+                                     "steps_timed": cpu_steps, "cores": threads}
+        rv = out["reference_cuda_kernels"].get("value")
+        if rv:
+            out["speedup_f32c_vs_reference_kernels"] = out["engine_f32c"]["value"] / rv
+            out["speedup_f64_vs_reference_kernels"] = out["engine_f64"]["value"] / rv
+        print(json.dumps(out), flush=True)
+
+
+def run_precision_study(a, local):
+    """64^3 lattice dropped on a frictional plane, dt = 1e-5: FP32 and FP32C
+    trajectories against the FP64 form over --study-steps steps (a bounded
+    horizon of the 10^6-step study), plus total energy of each."""
+    import numpy as np
+    import torch
+
+    import titan_gb300 as tg
+    from titan_gb300 import workloads as wl
+
+    torch.cuda.set_device(local)
+    sc = wl.config4()
+    n = sc["pos"].shape[0]
+    chunk = max(1, a.study_steps // 10)
+    sims = {p: wl.make_sim(sc, p, 0, device=local) for p in (tg.FP64, tg.FP32, tg.FP32C)}
+    g = float(abs(sc["g"][2]))
+    rows = []
+    done = 0
+    while done < a.study_steps:
+        k = min(chunk, a.study_steps - done)
+        for s in sims.values():
+            s.step(k)
+        done += k
+        st = {p: s.get_state(pos=True, vel=True) for p, s in sims.items()}
+        row = {"steps": done, "t": done * sc["dt"]}
+        for p, key in ((tg.FP32, "f32"), (tg.FP32C, "f32c")):
+            d = st[p]["pos"] - st[tg.FP64]["pos"]
+            row[key + "_max_pos_err_m"] = float(np.max(np.abs(d)))
+            row[key + "_rms_pos_err_m"] = float(np.sqrt(np.mean(d * d)))
+        for p, key in ((tg.FP64, "f64"), (tg.FP32, "f32"), (tg.FP32C, "f32c")):
+            row[key + "_energy_j"] = float(sims[p].diagnostics(g)["total"])
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+    for s in sims.values():
+        s.close()
+    print(json.dumps({"study": "64^3 lattice, dt=1e-5, plane mu 0.5", "masses": n, "steps": a.study_steps,
+                      "final": rows[-1]}), flush=True)
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
+    if a.suite:
+        if rank == 0:
+            run_suite(a, local)
+        return
+    if a.precision_study:
+        if rank == 0:
+            run_precision_study(a, local)
+        return
     if a.impl == "reference":
         res = run_reference(a, rank, world)
     else:

@@ -38,6 +38,7 @@ extern "C" {
 #define TITAN_GB300_ESTATE 5      /* simulation ended / not started       */
 #define TITAN_GB300_ETIMEOUT 6    /* a bounded wait gave up               */
 #define TITAN_GB300_EBUDGET 7     /* serving admission over HBM budget    */
+#define TITAN_GB300_EBUSY 8       /* poll: queued steps still running     */
 
 /* Arithmetic of the step.  FP64 is the drop-in form (reference kernels are
  * FP64).  FP32 runs positions/velocities in single precision.  FP32C runs the
@@ -193,6 +194,25 @@ int titan_gb300_step(titan_gb300_sim *sim, int64_t nsteps);
 
 /* Wait for queued work; replaces the cudaDeviceSynchronize at src/sim.cu:1570. */
 int titan_gb300_synchronize(titan_gb300_sim *sim);
+
+/* step() is the asynchronous rollout launch.  poll(): TITAN_GB300_OK when
+ * every queued step has finished, TITAN_GB300_EBUSY while some still run (a
+ * non-blocking replacement for the reference's running()/waitForEvent()
+ * spin, src/sim.cu:1628-1657).  wait(): blocks up to timeout_ms, then
+ * TITAN_GB300_ETIMEOUT with the work still queued. */
+int titan_gb300_poll(titan_gb300_sim *sim);
+int titan_gb300_wait(titan_gb300_sim *sim, double timeout_ms);
+
+/* Headless replacements of the reference's OpenGL export kernels.
+ * export_vertices: the positions of all masses in creation order as 3n
+ * floats, (float) of the position (updateVertices, src/sim.cu:1717-1725).
+ * export_indices: 2 * ns uint32 -- each spring's left and right mass index,
+ * (0, 0) for a spring without both masses (updateIndices,
+ * src/sim.cu:1727-1750).  out_on_device != 0: out is device memory and the
+ * vertex copy is queued on the handle's stream (no host synchronisation);
+ * else out is host memory and the call returns when it is filled. */
+int titan_gb300_export_vertices(titan_gb300_sim *sim, float *out, int out_on_device);
+int titan_gb300_export_indices(titan_gb300_sim *sim, uint32_t *out, int out_on_device);
 
 /* Replaces time() (src/sim.cu:1082): host-accumulated T (T += dt per step). */
 double titan_gb300_time(const titan_gb300_sim *sim);

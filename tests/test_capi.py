@@ -319,3 +319,20 @@ def test_set_occupancy_validates():
     s.set_occupancy(4)
     s.set_occupancy(0)
     s.close()
+
+
+def test_export_indices_on_host_before_start():
+    sc = wl.lattice_scene((0, 0, 1), (1, 1, 1), 3, 3, 3)
+    sc["left"] = np.concatenate([sc["left"], [-1, 5]]).astype(np.int32)
+    sc["right"] = np.concatenate([sc["right"], [4, -1]]).astype(np.int32)
+    for key, val in (("k", 1e3), ("rest", 0.1), ("damping", 0.0), ("omega", 0.0), ("amp", 0.2), ("phase", 0.0)):
+        sc[key] = np.concatenate([sc[key], [val] * 2])
+    sc["type"] = np.concatenate([sc["type"], [0, 0]]).astype(np.int32)
+    s = tg.Sim(tg.FP32C)
+    wl.load(s, sc, start=False)
+    idx = s.export_indices()
+    ns = sc["left"].size
+    assert idx.shape == (ns, 2)
+    assert (idx[:-2, 0] == sc["left"][:-2]).all() and (idx[:-2, 1] == sc["right"][:-2]).all()
+    assert (idx[-2:] == 0).all()  # detached springs export (0, 0)
+    s.close()

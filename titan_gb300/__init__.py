@@ -68,6 +68,10 @@ _SIGS = {
     "titan_gb300_resident_info": (ctypes.c_int, [_P, _I64]),
     "titan_gb300_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "titan_gb300_synchronize": (ctypes.c_int, [_P]),
+    "titan_gb300_poll": (ctypes.c_int, [_P]),
+    "titan_gb300_wait": (ctypes.c_int, [_P, ctypes.c_double]),
+    "titan_gb300_export_vertices": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_int]),
+    "titan_gb300_export_indices": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_int]),
     "titan_gb300_time": (ctypes.c_double, [_P]),
     "titan_gb300_steps": (ctypes.c_int64, [_P]),
     "titan_gb300_get_state": (ctypes.c_int, [_P, _D, _D, _D, _D]),
@@ -287,6 +291,46 @@ class Sim:
 
     def step(self, nsteps: int = 1):
         self._check(self._L.titan_gb300_step(self._h, nsteps), "step")
+
+    def poll(self) -> bool:
+        """True when every queued step has finished."""
+        rc = self._L.titan_gb300_poll(self._h)
+        if rc == 8:  # TITAN_GB300_EBUSY
+            return False
+        self._check(rc, "poll")
+        return True
+
+    def wait(self, timeout_ms: float) -> bool:
+        """Block up to timeout_ms; False when the steps are still running."""
+        rc = self._L.titan_gb300_wait(self._h, float(timeout_ms))
+        if rc == 6:  # TITAN_GB300_ETIMEOUT
+            return False
+        self._check(rc, "wait")
+        return True
+
+    def export_vertices(self, out=None, device_ptr: int = 0):
+        """float32 positions (n, 3) in creation order; with device_ptr, written
+        to that device address asynchronously instead."""
+        if device_ptr:
+            self._check(self._L.titan_gb300_export_vertices(self._h, ctypes.c_void_p(device_ptr), 1),
+                        "export_vertices")
+            return None
+        if out is None:
+            out = np.empty((self.n, 3), np.float32)
+        self._check(self._L.titan_gb300_export_vertices(self._h, out.ctypes.data_as(ctypes.c_void_p), 0),
+                    "export_vertices")
+        return out
+
+    def export_indices(self, device_ptr: int = 0):
+        """uint32 (ns, 2) left/right mass index of each spring ((0, 0) if detached)."""
+        if device_ptr:
+            self._check(self._L.titan_gb300_export_indices(self._h, ctypes.c_void_p(device_ptr), 1),
+                        "export_indices")
+            return None
+        out = np.empty((self.ns, 2), np.uint32)
+        self._check(self._L.titan_gb300_export_indices(self._h, out.ctypes.data_as(ctypes.c_void_p), 0),
+                    "export_indices")
+        return out
 
     def synchronize(self):
         self._check(self._L.titan_gb300_synchronize(self._h), "synchronize")

@@ -10,7 +10,9 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <chrono>
 #include <cstring>
+#include <thread>
 #include <map>
 #include <memory>
 #include <new>
@@ -528,7 +530,8 @@ int build_device(titan_gb300_sim *s) {
         W.idx_words = (int32_t)al(mNh, 4);
         W.heavy_cap = (int32_t)std::max<int64_t>(1, mH);
         const int64_t tail = 2 * (int64_t)W.idx_words * 4 + al(2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16) +
-                             (2 * tg::kWsMaxStages + 2) * 8 + 32;
+                             tg::kWsMaxStages * (int64_t)sizeof(tg::TileInfo) +
+                             al((int64_t)sizeof(tg::DevParams), 16) + (2 * tg::kWsMaxStages + 2) * 8 + 32;
         const int64_t room = 227 * 1024 - tail;
         W.nstages = (int32_t)std::min<int64_t>(tg::kWsMaxStages, room / std::max<int64_t>(1, W.stage));
         if (W.nstages < 2 && s->kernel_req == 4)
@@ -539,7 +542,9 @@ int build_device(titan_gb300_sim *s) {
         tg::WsLayout &W = a.ws;
         W.idx = W.nstages * W.stage;
         W.heavy = W.idx + 2 * W.idx_words * 4;
-        W.mbar = (int32_t)al(W.heavy + 2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16);
+        W.tinfo = (int32_t)al(W.heavy + 2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16);
+        W.params = W.tinfo + W.nstages * (int32_t)sizeof(tg::TileInfo);
+        W.mbar = (int32_t)al(W.params + (int64_t)sizeof(tg::DevParams), 16);
         W.total = W.mbar + (2 * W.nstages + 2) * 8 + 32;
         s->ws_warps = s->threads_req > 0 ? s->threads_req / 32 : tg::kWsMaxConsumerWarps;
         s->ws_warps = std::max(2, std::min(tg::kWsMaxConsumerWarps, s->ws_warps)) & ~1;
@@ -1116,6 +1121,74 @@ int titan_gb300_synchronize(titan_gb300_sim *s) {
     if (!s->stream) return TITAN_GB300_OK;
     CK(cudaStreamSynchronize(s->stream), "synchronize");
     return check_kernel_error(s);
+}
+
+int titan_gb300_poll(titan_gb300_sim *s) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->stream) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    const cudaError_t e = cudaStreamQuery(s->stream);
+    if (e == cudaErrorNotReady) return TITAN_GB300_EBUSY;
+    if (e != cudaSuccess) return s->cuda_fail(e, "poll");
+    return check_kernel_error(s);
+}
+
+int titan_gb300_wait(titan_gb300_sim *s, double timeout_ms) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!(timeout_ms >= 0)) return s->fail(TITAN_GB300_EINVAL, "timeout must be >= 0");
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const int rc = titan_gb300_poll(s);
+        if (rc != TITAN_GB300_EBUSY) return rc;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (ms >= timeout_ms) return s->fail(TITAN_GB300_ETIMEOUT, "queued steps still running at the time limit");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_device) {
+    if (!s || !out) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    tg::XferArgs x{};
+    x.old2new = s->d_old2new;
+    x.count = s->n;
+    x.npad = s->npad;
+    x.state0 = s->args.state0;
+    x.state1 = s->args.state1;
+    x.acc = s->args.acc;
+    x.parity = s->parity;
+    if (out_on_device) {
+        CK(tg::launch_export_f32(s->prec, x, out, s->stream), "export vertices");
+        return TITAN_GB300_OK;
+    }
+    // host buffer: through the staging area (9n doubles >= 3n floats)
+    float *d = reinterpret_cast<float *>(s->d_xfer);
+    CK(tg::launch_export_f32(s->prec, x, d, s->stream), "export vertices");
+    CK(cudaMemcpyAsync(out, d, 3 * (size_t)s->n * sizeof(float), cudaMemcpyDeviceToHost, s->stream),
+       "export vertices");
+    CK(cudaStreamSynchronize(s->stream), "export vertices");
+    return TITAN_GB300_OK;
+}
+
+int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_device) {
+    if (!s || !out) return TITAN_GB300_EINVAL;
+    std::vector<uint32_t> idx(2 * (size_t)s->ns, 0);
+    for (int64_t j = 0; j < s->ns; j++) {
+        const int32_t l = s->left[j], r = s->right[j];
+        if (l < 0 || r < 0 || l >= s->n || r >= s->n) continue;  // detached: (0, 0)
+        idx[2 * j] = (uint32_t)l;
+        idx[2 * j + 1] = (uint32_t)r;
+    }
+    if (!out_on_device) {
+        if (!idx.empty()) std::memcpy(out, idx.data(), idx.size() * sizeof(uint32_t));
+        return TITAN_GB300_OK;
+    }
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    if (!idx.empty())
+        CK(cudaMemcpy(out, idx.data(), idx.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "export indices");
+    return TITAN_GB300_OK;
 }
 
 double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }

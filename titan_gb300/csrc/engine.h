@@ -47,12 +47,13 @@ constexpr int kPipeTileCache = 64;
 // Shared-memory layout of the warp-specialised persistent kernel
 // (step_ws.cu): nstages stages, each [state records | slab records / force
 // slots | actuation records | incidence block], the two-entry halo-index
-// ring, the heavy-mass sums, then 2 * nstages + 2 mbarriers and the control
-// words.
+// ring, the heavy-mass sums, the TileInfo of each stage, a copy of the
+// DevParams, then 2 * nstages + 2 mbarriers and the control words.
 struct WsLayout {
     int32_t slots, act, inc, stage, nstages;  // offsets inside a stage, stage size
     int32_t idx, idx_words;                   // halo-index ring (2 entries of idx_words int32)
-    int32_t heavy, heavy_cap, mbar, total;    // heavy sums: 2 groups x 3 x heavy_cap
+    int32_t heavy, heavy_cap;                 // heavy sums: 2 groups x 3 x heavy_cap
+    int32_t tinfo, params, mbar, total;       // per-stage TileInfo, DevParams copy, barriers
 };
 constexpr int kWsMaxStages = 3;
 constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
@@ -69,6 +70,8 @@ struct DevParams {
     float planef[kMaxPlanes][6];
     float ballf[kMaxBalls][4];
 };
+
+static_assert(sizeof(DevParams) % 16 == 0, "DevParams is copied as 16-byte vectors");
 
 struct StepArgs {
     const TileInfo *tiles;
@@ -192,6 +195,8 @@ int resident_ctas_per_sm(int precision, int mpt, int threads, size_t smem);
 cudaError_t launch_resident(int precision, const StepArgs &a, const ResArgs &r, int ctas, int threads, int parity,
                             int64_t nsteps, int write_acc, int write_time, cudaStream_t s);
 cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
+// float positions of all a.count masses in caller order into out (device)
+cudaError_t launch_export_f32(int precision, const XferArgs &a, float *out, cudaStream_t s);
 cudaError_t launch_scatter(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_diag(int precision, const DiagArgs &a, cudaStream_t s);
 

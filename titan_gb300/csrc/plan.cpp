@@ -180,7 +180,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 work.emplace_front(lo, mid);
                 continue;
             }
-            // commit tile
+            // commit tile (slab: actuated entries first, each part in spring order)
             std::sort(ents_act.begin(), ents_act.end());
             std::sort(ents.begin(), ents.end());
             std::sort(halo.begin(), halo.end());

@@ -92,12 +92,16 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
     int *idx_issued = issued_word + 1, *idx_waited = issued_word + 2;
     int *last_word = issued_word + 3;                              // [2]: last tile each group consumed
     int32_t *idxbuf = reinterpret_cast<int32_t *>(smem + L.idx);  // 2 * L.idx_words
+    TileInfo *tinfo = reinterpret_cast<TileInfo *>(smem + L.tinfo);  // [NS]: the tile in each stage
     const uint8_t *in = reinterpret_cast<const uint8_t *>(parity ? a.state1 : a.state0);
     void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
-    const DevParams *prm = a.prm;
+    // the step's parameters, read per mass by the epilogue, from shared memory
+    DevParams *prm = reinterpret_cast<DevParams *>(smem + L.params);
+    for (int q = threadIdx.x; q < (int)(sizeof(DevParams) / 16); q += blockDim.x)
+        reinterpret_cast<int4 *>(prm)[q] = __ldg(reinterpret_cast<const int4 *>(a.prm) + q);
     const StepTime tm = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + prm->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + a.prm->dt;
     const int ncw = (int)(blockDim.x >> 5) - 1;  // consumer warps (even)
     const int gw = ncw >> 1;                     // warps per group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -157,6 +161,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
             }
             uint8_t *st = smem + (int64_t)s * L.stage;
             if (lane == 0) {
+                tinfo[s] = ti;  // published by the arrival below
                 fence_proxy_async();
                 const uint32_t eb = (uint32_t)ti.ne * kSlot, ab = (uint32_t)ti.nact * kSlot;
                 const uint32_t ib = (uint32_t)ti.inc_words * 2u, sb = (uint32_t)ti.nm * kRec;
@@ -191,9 +196,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
         for (int k = grp, t = blockIdx.x + grp * G; t < ntiles; k += 2, t += 2 * G) {
             const int s = k % NS;
             const uint32_t ph = (uint32_t)(k / NS) & 1u;
-            const TileInfo ti = a.tiles[t];
+            const bool ok = ws_wait(&full[s], ph, abort_word);
+            if (group_any(bar_id, gn, !ok)) {
+                if (gt == 0) {
+                    *abort_word = 1;
+                    atomicOr(a.err, 1);
+                }
+                break;
+            }
+            if (gt == 0) last_word[grp] = k;
+            const TileInfo ti = tinfo[s];
             const int E = ti.ne;
-            // per-mass scalars of this group's first masses, loaded while the copies land
+            // per-mass scalars of this group's first masses (needed in phase
+            // C; their loads overlap phase B)
             const int i_own = gt;
             uint8_t fl_own = MF_FIXED;
             uint32_t d_own = 0, woff_own = 0;
@@ -205,15 +220,6 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                 m_own = __ldg(reinterpret_cast<const R *>(a.mass) + g);
                 woff_own = __ldg(a.warp_inc_off + ti.warp_off + (i_own >> 5));
             }
-            const bool ok = ws_wait(&full[s], ph, abort_word);
-            if (group_any(bar_id, gn, !ok)) {
-                if (gt == 0) {
-                    *abort_word = 1;
-                    atomicOr(a.err, 1);
-                }
-                break;
-            }
-            if (gt == 0) last_word[grp] = k;
             uint8_t *st = smem + (int64_t)s * L.stage;
             uint8_t *slots = st + L.slots;
             const uint8_t *actb = st + L.act;

@@ -34,6 +34,23 @@ __global__ void k_gather(XferArgs a) {
     }
 }
 
+// Positions of all masses in caller (creation) order as float triples, the
+// headless form of the reference's updateVertices (src/sim.cu:1717-1725):
+// (float) of the position (FP32C: of hi + lo in double).
+template <int PREC>
+__global__ void k_export_f32(XferArgs a, float *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.count) return;
+    const int64_t g = a.old2new[i];
+    const St<PREC> s = load_state<PREC>(a.parity ? a.state1 : a.state0, g);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double x = (double)s.x[c];
+        if constexpr (PREC == P_FP32C) x += (double)s.xl[c];
+        out[3 * i + c] = (float)x;
+    }
+}
+
 // Writes pos and/or vel of the listed masses into both buffers, keeping the
 // other field from the current buffer.
 template <int PREC>
@@ -138,6 +155,17 @@ __global__ void __launch_bounds__(256) k_diag2(DiagArgs a) {
 
 }  // namespace
 
+
+cudaError_t launch_export_f32(int precision, const XferArgs &a, float *out, cudaStream_t s) {
+    if (a.count <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((a.count + 255) / 256);
+    switch (precision) {
+        case P_FP64: k_export_f32<P_FP64><<<blocks, 256, 0, s>>>(a, out); break;
+        case P_FP32: k_export_f32<P_FP32><<<blocks, 256, 0, s>>>(a, out); break;
+        default: k_export_f32<P_FP32C><<<blocks, 256, 0, s>>>(a, out); break;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s) {
     if (a.count <= 0) return cudaSuccess;
