@@ -59,6 +59,11 @@ def parse():
     p.add_argument("--precision-study", action="store_true",
                    help="instead of the headline line: 64^3 lattice at dt=1e-5, FP32 and FP32C against FP64")
     p.add_argument("--study-steps", type=int, default=20000)
+    p.add_argument("--serving", action="store_true",
+                   help="instead of the headline line: rollout serving, Poisson arrivals (p50/p99 latency)")
+    p.add_argument("--serve-requests", type=int, default=400)
+    p.add_argument("--serve-rate", type=float, default=200.0)
+    p.add_argument("--serve-max-masses", type=int, default=200000)
     p.add_argument("--ref-gpu-steps", type=int, default=50,
                    help="steps of the reference's own CUDA kernels timed beside ours (0: skip)")
     return p.parse_args()
@@ -437,15 +442,26 @@ def run_precision_study(a, local):
     chunk = max(1, a.study_steps // 10)
     sims = {p: wl.make_sim(sc, p, 0, device=local) for p in (tg.FP64, tg.FP32, tg.FP32C)}
     g = float(abs(sc["g"][2]))
+    # the reference's own kernels (FP64, float atomics in scheduling order):
+    # their distance from the engine's FP64 trajectory is the spread the
+    # reference itself has between runs, the floor for any comparison
+    from oracle import refgpu
+    ref = None if refgpu.available() else refgpu.RefGpuSim(sc, local)
     rows = []
     done = 0
     while done < a.study_steps:
         k = min(chunk, a.study_steps - done)
         for s in sims.values():
             s.step(k)
+        if ref is not None:
+            ref.step(k)
         done += k
         st = {p: s.get_state(pos=True, vel=True) for p, s in sims.items()}
         row = {"steps": done, "t": done * sc["dt"]}
+        if ref is not None:
+            d = ref.state()["pos"] - st[tg.FP64]["pos"]
+            row["reference_kernels_max_pos_diff_m"] = float(np.max(np.abs(d)))
+            row["reference_kernels_rms_pos_diff_m"] = float(np.sqrt(np.mean(d * d)))
         for p, key in ((tg.FP32, "f32"), (tg.FP32C, "f32c")):
             d = st[p]["pos"] - st[tg.FP64]["pos"]
             row[key + "_max_pos_err_m"] = float(np.max(np.abs(d)))
@@ -456,13 +472,50 @@ def run_precision_study(a, local):
         print(json.dumps(row), flush=True)
     for s in sims.values():
         s.close()
+    if ref is not None:
+        ref.close()
     print(json.dumps({"study": "64^3 lattice, dt=1e-5, plane mu 0.5", "masses": n, "steps": a.study_steps,
                       "final": rows[-1]}), flush=True)
+
+
+def run_serving(a, local):
+    """Rollout serving: requests with Poisson arrivals (--serve-rate per s),
+    masses log-uniform in [27, --serve-max-masses] (cube side =
+    round(cbrt)), horizon U[100, 5000] steps, 120 GB HBM budget; latency from
+    arrival to the final positions on the host."""
+    import torch
+
+    import titan_gb300 as tg
+    from titan_gb300 import serving
+    from titan_gb300 import workloads as wl
+
+    torch.cuda.set_device(local)
+    prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
+    reqs = wl.config5(a.serve_requests, a.serve_rate, mass_range=(27, a.serve_max_masses))
+    # scenes built before the clock starts (request payloads arrive ready)
+    scenes = {r["id"]: wl.rollout_request(r["side"], r["seed"]) for r in reqs}
+    srv = serving.RolloutServer(prec, device=local)
+    # warm-up: one request per design, so that the served run measures
+    # steady state (plans, engines and graphs exist)
+    warm = {}
+    for r in reqs:
+        warm.setdefault(r["side"], dict(r, arrival_s=0.0, steps=100))
+    srv.run(list(warm.values()), scene_of=lambda r: scenes[r["id"]])
+    recs, stats = srv.run(reqs, scene_of=lambda r: scenes[r["id"]])
+    srv.close()
+    masses = sum(rec["masses"] for rec in recs.values())
+    print(json.dumps({"workload": "rollout serving", "requests": len(reqs), "rate_per_s": a.serve_rate,
+                      "mean_masses": masses / len(recs), "precision": a.precision, **stats,
+                      "unit": UNIT}), flush=True)
 
 
 def main():
     a = parse()
     rank, world, local = dist_env()
+    if a.serving:
+        if rank == 0:
+            run_serving(a, local)
+        return
     if a.suite:
         if rank == 0:
             run_suite(a, local)

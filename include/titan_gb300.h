@@ -139,6 +139,15 @@ int titan_gb300_set_body_plane(titan_gb300_sim *sim, int64_t body, const double 
  * the tuned default. */
 int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
 
+/* Takes src's tile plan for this handle's next start() instead of building
+ * one (no reference counterpart: for serving many scenes of one topology).
+ * src must have been planned (plan_host) or started; both handles must have
+ * the same precision, kernel form, masses, springs (ends), fixed masses,
+ * actuated springs and bodies -- positions, parameters and constraints may
+ * differ.  The plan is used when start()'s tile size equals src's.  Results
+ * do not depend on which plan a scene runs with. */
+int titan_gb300_adopt_plan(titan_gb300_sim *sim, const titan_gb300_sim *src);
+
 /* Launch shape of the step kernel: threads per CTA, a multiple of 32 in
  * [64, 512], or 0 to derive it from the tile size.  Set before start(); the
  * tile size itself is start()'s argument.  Used by the autotuner. */
@@ -216,6 +225,9 @@ int titan_gb300_export_indices(titan_gb300_sim *sim, uint32_t *out, int out_on_d
 
 /* Replaces time() (src/sim.cu:1082): host-accumulated T (T += dt per step). */
 double titan_gb300_time(const titan_gb300_sim *sim);
+
+/* Device memory held by the handle (bytes), for admission control. */
+int64_t titan_gb300_device_bytes(const titan_gb300_sim *sim);
 
 /* Number of steps run since start(). */
 int64_t titan_gb300_steps(const titan_gb300_sim *sim);

@@ -60,6 +60,8 @@ _SIGS = {
     "titan_gb300_set_body_plane": (ctypes.c_int, [_P, ctypes.c_int64, _D, ctypes.c_double, ctypes.c_double,
                                                   ctypes.c_double]),
     "titan_gb300_start": (ctypes.c_int, [_P, ctypes.c_int]),
+    "titan_gb300_adopt_plan": (ctypes.c_int, [_P, _P]),
+    "titan_gb300_plan_host": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_launch": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_kernel": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_set_occupancy": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -73,6 +75,8 @@ _SIGS = {
     "titan_gb300_export_vertices": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_int]),
     "titan_gb300_export_indices": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_int]),
     "titan_gb300_time": (ctypes.c_double, [_P]),
+    "titan_gb300_set_time": (ctypes.c_int, [_P, ctypes.c_double]),
+    "titan_gb300_device_bytes": (ctypes.c_int64, [_P]),
     "titan_gb300_steps": (ctypes.c_int64, [_P]),
     "titan_gb300_get_state": (ctypes.c_int, [_P, _D, _D, _D, _D]),
     "titan_gb300_get_masses": (ctypes.c_int, [_P, ctypes.c_int64, _I64, _D, _D, _D, _D]),
@@ -233,6 +237,13 @@ class Sim:
     def clear_constraints(self):
         self._check(self._L.titan_gb300_clear_constraints(self._h), "clear_constraints")
 
+    def set_time(self, T: float):
+        """Set the simulation clock (the time actuation sees)."""
+        self._check(self._L.titan_gb300_set_time(self._h, float(T)), "set_time")
+
+    def device_bytes(self) -> int:
+        return int(self._L.titan_gb300_device_bytes(self._h))
+
     def set_time_step(self, dt):
         self._check(self._L.titan_gb300_set_time_step(self._h, dt), "set_time_step")
 
@@ -285,6 +296,14 @@ class Sim:
         self._check(self._L.titan_gb300_resident_info(self._h, _ptr(out, ctypes.c_int64)), "resident_info")
         keys = ("active", "bins", "bodies", "masses", "cap", "threads", "ctas", "smem_bytes")
         return {k: int(v) for k, v in zip(keys, out)}
+
+    def plan_host(self, tile_masses: int = 0):
+        """Build the tile plan on the host only (no GPU needed)."""
+        self._check(self._L.titan_gb300_plan_host(self._h, tile_masses), "plan_host")
+
+    def adopt_plan(self, src: "Sim"):
+        """Use src's plan (same topology) for the next start()."""
+        self._check(self._L.titan_gb300_adopt_plan(self._h, src._h), "adopt_plan")
 
     def start(self, tile_masses: int = 0):
         self._check(self._L.titan_gb300_start(self._h, tile_masses), "start")

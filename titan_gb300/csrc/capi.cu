@@ -38,16 +38,21 @@ double norm3(const double *v) {
 
 struct DevMem {
     std::vector<void *> ptrs;
+    size_t total = 0;
     void *get(size_t bytes, cudaError_t &e) {
         void *p = nullptr;
         if (bytes == 0) bytes = 16;
         e = cudaMalloc(&p, bytes);
-        if (e == cudaSuccess) ptrs.push_back(p);
+        if (e == cudaSuccess) {
+            ptrs.push_back(p);
+            total += bytes;
+        }
         return p;
     }
     void release() {
         for (void *p : ptrs) cudaFree(p);
         ptrs.clear();
+        total = 0;
     }
 };
 
@@ -125,6 +130,10 @@ struct titan_gb300_sim {
     tg::ResArgs rargs{};
     bool use_res = false;
     int res_threads = 0, res_ctas = 0;
+    // plan taken from another handle with the same topology (adopt_plan);
+    // used by the first start() only
+    bool plan_adopted = false;
+    int plan_tile = 0;  // tile size the current plan was built with
 
     cudaError_t launch(int parity, int write_acc) {
         if (args.ntiles == 0) return cudaSuccess;
@@ -405,8 +414,14 @@ int build_device(titan_gb300_sim *s) {
     s->free_device();
     tg::PlanInput in = plan_input(s, s->tile_masses);
     const size_t rs = s->rsize();
-    std::string why = tg::build_plan(in, s->plan);
-    if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    if (s->plan_adopted && !s->started && s->plan_tile == in.tile_cap) {
+        s->plan_adopted = false;  // the adopted plan serves this first start
+    } else {
+        s->plan_adopted = false;
+        std::string why = tg::build_plan(in, s->plan);
+        if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+        s->plan_tile = in.tile_cap;
+    }
     const tg::Plan &P = s->plan;
     s->threads = s->threads_req > 0 ? s->threads_req : std::max(128, std::min(512, ((P.max_nm + 31) / 32) * 32));
     s->npad = ((s->n + 127) / 128) * 128;
@@ -851,6 +866,26 @@ int titan_gb300_resident_info(const titan_gb300_sim *s, int64_t out[8]) {
     return TITAN_GB300_OK;
 }
 
+int titan_gb300_adopt_plan(titan_gb300_sim *s, const titan_gb300_sim *src) {
+    if (!s || !src) return TITAN_GB300_EINVAL;
+    if (s->started) return s->fail(TITAN_GB300_ESTATE, "adopt a plan before start");
+    if (src->plan.ntiles <= 0) return s->fail(TITAN_GB300_EINVAL, "the source handle has no plan");
+    auto flags = [](const titan_gb300_sim *h, int64_t i) { return !h->fixed.empty() && h->fixed[i] != 0; };
+    auto act = [](const titan_gb300_sim *h, int64_t j) { return !h->type.empty() && h->type[j] >= 2; };
+    bool same = s->prec == src->prec && s->n == src->n && s->ns == src->ns && s->left == src->left &&
+                s->right == src->right && s->body_ptr == src->body_ptr && s->kernel_req == src->kernel_req;
+    for (int64_t i = 0; same && i < s->n; i++) same = flags(s, i) == flags(src, i);
+    for (int64_t j = 0; same && j < s->ns; j++) same = act(s, j) == act(src, j);
+    if (!same)
+        return s->fail(TITAN_GB300_EINVAL,
+                       "adopt_plan needs the same precision, kernel form, masses, springs, fixed masses, "
+                       "actuated springs and bodies");
+    s->plan = src->plan;
+    s->plan_tile = src->plan_tile;
+    s->plan_adopted = true;
+    return TITAN_GB300_OK;
+}
+
 int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
     if (!s) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "plan_host is for scenes that have not started");
@@ -858,6 +893,8 @@ int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
     tg::PlanInput in = plan_input(s, tile_masses);
     std::string why = tg::build_plan(in, s->plan);
     if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    s->plan_tile = in.tile_cap;
+    s->plan_adopted = false;
     s->rplan = tg::ResPlan();
     const int cap = resident_cap(s);
     if (cap > 0) tg::build_resident(in, s->plan, cap, cap, s->rplan);
@@ -911,6 +948,7 @@ const char *titan_gb300_last_error(const titan_gb300_sim *s) {
 int titan_gb300_set_masses(titan_gb300_sim *s, int64_t n, const double *pos, const double *vel,
                            const double *m, const double *ext, const uint8_t *fixed, const double *drag) {
     if (!s) return TITAN_GB300_EINVAL;
+    s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "masses can only be replaced before start");
     if (n <= 0 || !pos || !m) return s->fail(TITAN_GB300_EINVAL, "need n > 0, pos and m");
     s->n = n;
@@ -938,6 +976,7 @@ int titan_gb300_set_springs(titan_gb300_sim *s, int64_t n, const int32_t *left, 
                             const int32_t *type, const double *omega, const double *amp,
                             const double *phase) {
     if (!s) return TITAN_GB300_EINVAL;
+    s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "springs can only be replaced before start");
     if (n < 0 || (n > 0 && (!left || !right || !k || !rest))) return s->fail(TITAN_GB300_EINVAL, "bad springs");
     s->ns = n;
@@ -1040,6 +1079,7 @@ int titan_gb300_set_global_acc(titan_gb300_sim *s, const double g[3]) {
 
 int titan_gb300_set_bodies(titan_gb300_sim *s, int64_t nbodies, const int64_t *mass_ptr) {
     if (!s) return TITAN_GB300_EINVAL;
+    s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set bodies before start");
     if (nbodies <= 0 || !mass_ptr || mass_ptr[0] != 0 || mass_ptr[nbodies] != s->n)
         return s->fail(TITAN_GB300_EINVAL, "body ranges must cover all masses");
@@ -1192,6 +1232,8 @@ int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_dev
 }
 
 double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }
+
+int64_t titan_gb300_device_bytes(const titan_gb300_sim *s) { return s ? (int64_t)s->mem.total : 0; }
 
 int titan_gb300_set_time(titan_gb300_sim *s, double T) {
     if (!s) return TITAN_GB300_EINVAL;

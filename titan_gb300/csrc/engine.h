@@ -153,6 +153,12 @@ struct DiagArgs {
 constexpr int kDiagBlocks = 512;
 constexpr int kDiagQ = 9;
 
+// Raises kernel f's dynamic shared-memory limit on the current device to at
+// least smem bytes, never lowering it: several engine handles in one process
+// share the kernels, and a handle that needs less must not shrink the limit
+// another handle's launches rely on.
+cudaError_t raise_smem_limit(const void *f, size_t smem);
+
 // words (of the precision's scalar) in one mass's state record
 int state_words(int precision);
 // dynamic shared memory of one tile's CTA

@@ -213,7 +213,7 @@ size_t resident_smem_bytes(int precision, int cap) {
 
 cudaError_t resident_prepare(int precision, int mpt, size_t smem) {
     if (mpt < 1 || mpt > kResMaxMpt) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(res_kernel(precision, mpt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return raise_smem_limit(res_kernel(precision, mpt), smem);
 }
 
 int resident_ctas_per_sm(int precision, int mpt, int threads, size_t smem) {

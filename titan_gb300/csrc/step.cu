@@ -2,10 +2,27 @@
 // FP64 form and the default launch bounds of every precision; the
 // register-capped variants of the FP32 forms are in step_var.cu.
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "step_kernel.cuh"
 
 namespace tg {
+
+cudaError_t raise_smem_limit(const void *f, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> limit;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = limit[{dev, f}];
+    if (smem <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) cur = smem;
+    return e;
+}
 
 int state_words(int precision) { return precision == P_FP64 ? 6 : (precision == P_FP32C ? 12 : 8); }
 
@@ -26,7 +43,7 @@ const void *step_kernel(int precision, int variant) {
 cudaError_t step_prepare(int precision, int variant, size_t smem) {
     const void *f = step_kernel(precision, variant);
     if (!f) return cudaErrorInvalidValue;
-    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return raise_smem_limit(f, smem);
 }
 
 cudaError_t launch_step(int precision, int variant, const StepArgs &a, int ntiles, int threads, size_t smem,

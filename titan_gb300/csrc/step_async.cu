@@ -181,7 +181,7 @@ cudaError_t step_async_prepare(int precision, size_t smem) {
     const void *f = precision == P_FP64   ? (const void *)k_step_async<P_FP64>
                     : precision == P_FP32 ? (const void *)k_step_async<P_FP32>
                                           : (const void *)k_step_async<P_FP32C>;
-    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return raise_smem_limit(f, smem);
 }
 
 cudaError_t launch_step_async(int precision, const StepArgs &a, int ntiles, int threads, size_t smem, int parity,

@@ -257,7 +257,7 @@ cudaError_t step_pipe_prepare(int precision, size_t smem) {
     const void *f = precision == P_FP64   ? (const void *)k_step_pipe<P_FP64>
                     : precision == P_FP32 ? (const void *)k_step_pipe<P_FP32>
                                           : (const void *)k_step_pipe<P_FP32C>;
-    return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return raise_smem_limit(f, smem);
 }
 
 cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int threads, int parity, int write_acc,

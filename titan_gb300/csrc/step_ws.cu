@@ -311,7 +311,7 @@ const void *ws_kernel(int precision) {
 }  // namespace
 
 cudaError_t step_ws_prepare(int precision, size_t smem) {
-    return cudaFuncSetAttribute(ws_kernel(precision), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return raise_smem_limit(ws_kernel(precision), smem);
 }
 
 cudaError_t launch_step_ws(int precision, const StepArgs &a, int ctas, int consumer_warps, int parity,

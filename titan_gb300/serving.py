@@ -1,0 +1,142 @@
+"""Rollout serving over the engine: many independent scenes (requests) on
+one GPU, each rolled out for its own number of steps and returned to the host.
+
+Design (GB300-first, no reference counterpart -- the reference runs one scene
+per process):
+  * every active request runs on its own engine handle and CUDA stream, so
+    the GPU executes the steps of all active requests concurrently (kernels
+    from different streams overlap); step() is asynchronous and completion is
+    detected with poll(), so one host thread keeps many rollouts in flight;
+  * admission control: a request starts only while the device bytes of all
+    active requests stay within the HBM budget (default 120 GB), and at most
+    max_active run at once; the rest wait in arrival order;
+  * engines are pooled per design (identical topology): a finished engine is
+    reused for the next request of its design by uploading that request's
+    state, spring parameters and clock (no reallocation, no replanning, the
+    CUDA graphs stay cached), and the first engine of a design takes its
+    plan from a host-planned template (adopt_plan);
+  * a request's result is the same bits whether it runs alone or among
+    others: its engine's arithmetic depends only on its own scene.
+"""
+from __future__ import annotations
+
+import collections
+import time
+
+import numpy as np
+
+from . import FP32C, Sim
+from . import workloads as wl
+
+
+class RolloutServer:
+    def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_active=256, pool_per_design=64):
+        self.precision = precision
+        self.device = device
+        self.budget = float(hbm_budget_bytes)
+        self.max_active = max_active
+        self.pool_per_design = pool_per_design
+        self.templates = {}                          # side -> planned host-only Sim
+        self.pool = collections.defaultdict(list)    # side -> idle started engines
+        self.bytes_of = {}                           # side -> device bytes of one engine
+        self.used = 0.0
+        self.engines_built = 0
+
+    # -- engines ---------------------------------------------------------
+    def _estimate(self, side, sc):
+        if side in self.bytes_of:
+            return self.bytes_of[side]
+        n, ns = sc["pos"].shape[0], sc["left"].size
+        return 400.0 * n + 96.0 * ns + (8 << 20)
+
+    def _engine(self, side, sc):
+        """An engine loaded with scene sc, ready at time 0."""
+        if self.pool[side]:
+            e = self.pool[side].pop()
+            n = e.n
+            e.set_mass_state(None, pos=sc["pos"], vel=sc["vel"], T=np.zeros(n))
+            e.set_spring_params(None, k=sc["k"], rest=sc["rest"], damping=sc["damping"], type=sc["type"],
+                                omega=sc["omega"], amp=sc["amp"], phase=sc["phase"])
+            e.set_time(0.0)
+            return e
+        if side not in self.templates:
+            t = Sim(self.precision, self.device)
+            wl.load(t, sc, start=False)
+            t.plan_host()
+            self.templates[side] = t
+        e = Sim(self.precision, self.device)
+        wl.load(e, sc, start=False)
+        e.adopt_plan(self.templates[side])
+        e.start()
+        self.engines_built += 1
+        if side not in self.bytes_of:
+            self.bytes_of[side] = float(e.device_bytes())
+        return e
+
+    def _release(self, side, e):
+        if len(self.pool[side]) < self.pool_per_design:
+            self.pool[side].append(e)
+        else:
+            e.close()
+
+    # -- serving loop ----------------------------------------------------
+    def run(self, requests, scene_of=None, keep_results=False, time_scale=1.0):
+        """Serve requests (dicts with id, arrival_s, side, steps, seed) with
+        arrivals replayed in wall-clock time (arrival_s * time_scale).
+        Returns per-request records and summary statistics."""
+        scene_of = scene_of or (lambda r: wl.rollout_request(r["side"], r["seed"]))
+        pending = collections.deque(sorted(requests, key=lambda r: r["arrival_s"]))
+        active = []
+        records = {}
+        springs_done = 0
+        t0 = time.perf_counter()
+        while pending or active:
+            now = time.perf_counter() - t0
+            progressed = False
+            while pending and pending[0]["arrival_s"] * time_scale <= now and len(active) < self.max_active:
+                r = pending[0]
+                sc = scene_of(r)
+                need = self._estimate(r["side"], sc)
+                if active and self.used + need > self.budget:
+                    break  # admission by HBM budget: wait for a rollout to finish
+                pending.popleft()
+                e = self._engine(r["side"], sc)
+                e.step(r["steps"])
+                self.used += need
+                active.append((r, e, need, time.perf_counter() - t0, sc["left"].size))
+                progressed = True
+            still = []
+            for r, e, need, started, ns in active:
+                if e.poll():
+                    pos = e.get_state(pos=True, vel=False)["pos"]
+                    done = time.perf_counter() - t0
+                    rec = {"id": r["id"], "arrival_s": r["arrival_s"] * time_scale, "start_s": started,
+                           "done_s": done, "latency_ms": (done - r["arrival_s"] * time_scale) * 1e3,
+                           "steps": r["steps"], "masses": pos.shape[0], "springs": ns}
+                    if keep_results:
+                        rec["pos"] = pos
+                    records[r["id"]] = rec
+                    springs_done += ns * r["steps"]
+                    self.used -= need
+                    self._release(r["side"], e)
+                    progressed = True
+                else:
+                    still.append((r, e, need, started, ns))
+            active = still
+            if not progressed:
+                time.sleep(50e-6)
+        wall = time.perf_counter() - t0
+        lat = np.array([rec["latency_ms"] for rec in records.values()])
+        stats = {"requests": len(records), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                 "spring_updates_per_s": springs_done / wall, "engines_built": self.engines_built}
+        return records, stats
+
+    def close(self):
+        for lst in self.pool.values():
+            for e in lst:
+                e.close()
+        self.pool.clear()
+        for t in self.templates.values():
+            t.close()
+        self.templates.clear()

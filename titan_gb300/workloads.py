@@ -189,3 +189,63 @@ def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0, res
 def make_sim(sc: dict, precision=FP64, tile_masses=0, device=0, threads=0, kernel=0, resident=None,
              occupancy=0) -> Sim:
     return load(Sim(precision, device), sc, True, tile_masses, threads, kernel, resident, occupancy)
+
+
+def robot_design(side, spacing=0.1, design_seed=None):
+    """Topology of one soft-robot design of side^3 masses: a lattice with 5% of
+    springs removed and 30% of the rest actuated (type 2 or 3), chosen by a
+    seed derived from the side, so every rollout of a design shares one tile
+    plan.  Returns (pos, left, right, rest, actuated type)."""
+    rng = np.random.default_rng(1000003 + side if design_seed is None else design_seed)
+    pos, left, right, rest = lattice((0.0, 0.0, 0.05 + spacing * (side - 1) / 2), (spacing * (side - 1),) * 3,
+                                     side, side, side)
+    keep = rng.random(left.size) >= 0.05
+    left, right, rest = left[keep], right[keep], rest[keep]
+    typ = np.zeros(left.size, np.int32)
+    act = rng.random(left.size) < 0.3
+    typ[act] = rng.choice(np.array([2, 3], np.int32), size=int(act.sum()))
+    return pos, left, right, rest, typ
+
+
+_DESIGNS = {}
+
+
+def rollout_request(side, seed, dt=1e-4):
+    """One rollout request on design `side`: per-request spring constants
+    (log-uniform [1e3, 1e5]), actuation (amplitude 0.1, random phase, period
+    U[0.1, 1] s), initial velocity jitter; ground plane z = 0, friction 0.5,
+    damping 0.1."""
+    if side not in _DESIGNS:
+        _DESIGNS[side] = robot_design(side)
+    pos, left, right, rest, typ = _DESIGNS[side]
+    rng = np.random.default_rng(seed)
+    ns = left.size
+    act = typ >= 2
+    na = int(act.sum())
+    amp = np.full(ns, 0.2)
+    ph = np.zeros(ns)
+    om = np.zeros(ns)
+    amp[act] = 0.1
+    ph[act] = rng.uniform(0, TWO_PI, na)
+    om[act] = TWO_PI / rng.uniform(0.1, 1.0, na)
+    sc = empty_scene(dt)
+    sc.update(pos=pos.copy(), vel=rng.normal(scale=0.01, size=pos.shape), m=np.full(pos.shape[0], 0.1), left=left,
+              right=right, rest=rest, k=np.exp(rng.uniform(math.log(1e3), math.log(1e5), ns)),
+              damping=np.full(ns, 0.1), type=typ, omega=om, amp=amp, phase=ph)
+    sc["planes"].append(((0.0, 0.0, 1.0), 0.0, 0.5, 0.5))
+    return sc
+
+
+def config5(nreq, rate, seed=5, mass_range=(27, 200000), horizon=(100, 5000)):
+    """Serving workload: nreq rollout requests with Poisson arrivals at `rate`
+    per second, masses log-uniform in mass_range (cube side =
+    round(cbrt(masses))), horizon U[horizon] steps.  Returns a list of dicts
+    (id, arrival_s, side, steps, seed); scenes are built on demand by
+    rollout_request(side, seed)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    m = np.exp(rng.uniform(math.log(mass_range[0]), math.log(mass_range[1]), nreq))
+    sides = np.maximum(2, np.round(np.cbrt(m))).astype(int)
+    steps = rng.integers(horizon[0], horizon[1] + 1, nreq)
+    return [{"id": i, "arrival_s": float(t[i]), "side": int(sides[i]), "steps": int(steps[i]),
+             "seed": int(seed * 1000003 + i)} for i in range(nreq)]
