@@ -74,6 +74,23 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(x: float, world: int, device="cuda") -> float:
+    """The slowest rank's time: replicas report the whole job by it."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, world: int, max_seconds: float) -> float:
+    """Whole-job throughput of weak-scaled replicas: every rank processes
+    units_per_rank; the job takes as long as its slowest rank."""
+    return units_per_rank * world / max_seconds
+
+
 def peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -200,13 +217,6 @@ def run_ours(a, rank, world, local):
             import torch.distributed as dist
             dist.barrier()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
     sc = wl.config2(a.side)
@@ -233,13 +243,13 @@ def run_ours(a, rank, world, local):
     sim.synchronize()
     with ClockSampler(local) as clk:
         ms = timed(sim, a.steps)
-    ms_max = max_over_ranks(ms)
+    ms_max = max_over_ranks(ms, world)
     st = sim.get_state(pos=True, vel=False)
     finite = bool(np.all(np.isfinite(st["pos"])))
     per_launch_s = ms / a.steps / 1e3
     alg = info["algorithmic_bytes_per_step"]
     achieved = alg / per_launch_s / 1e9
-    value = ns * a.steps * world / (ms_max / 1e3)
+    value = replica_value(ns * a.steps, world, ms_max / 1e3)
     traffic = profiled_traffic(a.precision)
 
     # end to end through the C ABI with host buffers
@@ -255,7 +265,7 @@ def run_ours(a, rank, world, local):
         sim.set_mass_state(None, pos=pos_h, vel=vel_h)
         sim.step(a.e2e_chunk)
         sim.get_state(pos=True, vel=False, out=out)
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     barrier()
     e2e_val = ns * a.e2e_chunk * a.e2e_calls * world / e2e_s
     sim.close()
