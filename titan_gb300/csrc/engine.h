@@ -1,16 +1,19 @@
 // engine.h -- device-side layout shared by the step kernels and the C ABI.
 //
 // HBM layout (all arrays in the tiled mass order of plan.h):
-//   state[2]   ping-pong buffers, component-major with stride npad:
-//              FP64  : x0 x1 x2 v0 v1 v2                      (double)
-//              FP32  : x0 x1 x2 v0 v1 v2                      (float)
-//              FP32C : xh0..2 vh0..2 xl0..2 vl0..2            (float hi/lo pairs)
+//   state[2]   ping-pong buffers of per-mass records (state.cuh):
+//              FP64  48 B: x0 x1 | x2 v0 | v1 v2               (double)
+//              FP32C 48 B: xh0 xh1 xh2 vh0 | vh1 vh2 xl0 xl1 | xl2 vl0 vl1 vl2
+//                          (float hi/lo pairs)
+//              FP32  32 B: x0 x1 x2 v0 | v1 v2 - -             (float)
 //   mass, flags  per-mass m and MF_* bits; ext/lc/drag are only read for
-//              masses whose flag asks for them.
-//   tiles      one TileInfo per CTA.
+//              masses whose flag asks for them; acc component-major (npad).
+//   tiles      one TileInfo per tile.
 //   ent        slab entries: FP64 {k, rest, damping, ends} (32 B),
-//              FP32 {ends, k, rest, damping} (16 B); act: {omega, amp, phase}.
-//   inc        per-warp ELL incidence (u16 entry index, 0x8000 = left end).
+//              FP32 {ends, k, rest, damping} (16 B); act parallel:
+//              FP64 {omega, amp, phase, -}, FP32 {omega/2pi, +-amp, phase/2pi, -}.
+//   inc        per-warp ELL incidence (u16 entry index, 0x8000 = left end),
+//              4 codes per 8-byte word.
 #pragma once
 
 #include <cstddef>
