@@ -114,6 +114,17 @@ int titan_gb300_add_ball(titan_gb300_sim *sim, const double center[3], double ra
 /* Replaces clearConstraints (src/sim.cu:2037-2040): removes global planes and balls. */
 int titan_gb300_clear_constraints(titan_gb300_sim *sim);
 
+/* Integrator of the mass update: 0 = symplectic Euler (the reference's
+ * default build, src/sim.cu:1161-1166), 1 = VERLET (its -DVERLET build,
+ * :1155-1159; the acceleration is state and starts at 0), 2 = RK2 (its -DRK2
+ * build, :1141-1154 and :1572-1583: spring forces at T and at T + dt/2, time
+ * advanced by dt/2 twice per step).  The reference chooses at compile time;
+ * here it may change between steps.  Resident bins run Euler only. */
+#define TITAN_GB300_EULER 0
+#define TITAN_GB300_VERLET 1
+#define TITAN_GB300_RK2 2
+int titan_gb300_set_integrator(titan_gb300_sim *sim, int kind);
+
 /* Replaces setTimeStep (src/sim.cu:797-807); dt <= 0 is EINVAL. */
 int titan_gb300_set_time_step(titan_gb300_sim *sim, double dt);
 double titan_gb300_get_time_step(const titan_gb300_sim *sim);

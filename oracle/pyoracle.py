@@ -40,6 +40,7 @@ class ToScene(ctypes.Structure):
         ("mass_bp", _I32), ("bp_n", _D), ("bp_off", _D), ("bp_fk", _D), ("bp_fs", _D),
         ("g", ctypes.c_double * 3), ("dt", ctypes.c_double), ("T_global", ctypes.c_double),
         ("heavy_threshold", ctypes.c_int32),
+        ("integrator", ctypes.c_int32),
     ]
 
 
@@ -174,6 +175,7 @@ class OracleSim:
         s.dt = float(sc["dt"])
         s.T_global = 0.0
         s.heavy_threshold = heavy_threshold
+        s.integrator = int(sc.get("integrator", 0))
         self.s = s
 
     def _local(self, sc):

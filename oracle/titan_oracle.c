@@ -173,8 +173,9 @@ void to_direction_apply(const double t[3], double friction, double vel[3], doubl
     }
 }
 
-/* Per-mass part of src/sim.cu:1096-1168 (CONSTRAINTS on, symplectic Euler). */
-static void mass_update(to_scene *s, int64_t i) {
+/* Per-mass part of src/sim.cu:1096-1168 (CONSTRAINTS on).  stage: RK2's
+ * first (0) or second (1) half step; bx, bv: RK2 backups of this mass. */
+static void mass_update(to_scene *s, int64_t i, int stage, double *bx, double *bv) {
     if (s->fixed && s->fixed[i]) return;
     double *F = s->force + 3 * i;
     double *x = s->pos + 3 * i;
@@ -221,19 +222,41 @@ static void mass_update(to_scene *s, int64_t i) {
         F[1] = F[1] + (v[1] * c) / nv;
         F[2] = F[2] + (v[2] * c) / nv;
     }
-    double a0 = F[0] / m, a1 = F[1] / m, a2 = F[2] / m;
-    if (s->acc) {
-        s->acc[3 * i] = a0;
-        s->acc[3 * i + 1] = a1;
-        s->acc[3 * i + 2] = a2;
+    const double dt = s->dt;
+    double a[3] = {F[0] / m, F[1] / m, F[2] / m};
+    if (s->integrator == TO_VERLET) {  /* src/sim.cu:1155-1159 */
+        double *ac = s->acc + 3 * i;
+        const double dt2 = pow(dt, 2);
+        for (int c = 0; c < 3; c++) v[c] = v[c] + (0.5 * (ac[c] + a[c])) * dt;
+        for (int c = 0; c < 3; c++) ac[c] = a[c];
+        for (int c = 0; c < 3; c++) x[c] = x[c] + (v[c] * dt + (0.5 * ac[c]) * dt2);
+        if (s->T) s->T[i] = s->T[i] + dt;
+    } else if (s->integrator == TO_RK2) {  /* src/sim.cu:1141-1154 */
+        if (s->acc)
+            for (int c = 0; c < 3; c++) s->acc[3 * i + c] = a[c];
+        if (stage == 0) {
+            for (int c = 0; c < 3; c++) {
+                bv[c] = v[c];
+                bx[c] = x[c];
+            }
+            for (int c = 0; c < 3; c++) x[c] = x[c] + (0.5 * v[c]) * dt;
+            for (int c = 0; c < 3; c++) v[c] = v[c] + (0.5 * a[c]) * dt;
+        } else {
+            for (int c = 0; c < 3; c++) x[c] = bx[c] + v[c] * dt;
+            for (int c = 0; c < 3; c++) v[c] = bv[c] + a[c] * dt;
+        }
+        if (s->T) s->T[i] = s->T[i] + 0.5 * dt;
+    } else {  /* symplectic Euler, src/sim.cu:1161-1166 */
+        if (s->acc)
+            for (int c = 0; c < 3; c++) s->acc[3 * i + c] = a[c];
+        v[0] = v[0] + a[0] * dt;
+        v[1] = v[1] + a[1] * dt;
+        v[2] = v[2] + a[2] * dt;
+        x[0] = x[0] + v[0] * dt;
+        x[1] = x[1] + v[1] * dt;
+        x[2] = x[2] + v[2] * dt;
+        if (s->T) s->T[i] = s->T[i] + dt;
     }
-    v[0] = v[0] + a0 * s->dt;
-    v[1] = v[1] + a1 * s->dt;
-    v[2] = v[2] + a2 * s->dt;
-    x[0] = x[0] + v[0] * s->dt;
-    x[1] = x[1] + v[1] * s->dt;
-    x[2] = x[2] + v[2] * s->dt;
-    if (s->T) s->T[i] = s->T[i] + s->dt;
     F[0] = 0.0;
     F[1] = 0.0;
     F[2] = 0.0;
@@ -301,6 +324,8 @@ static void free_incidence(inc_list *L) {
 }
 
 int to_step(to_scene *s, int64_t nsteps, int order, int nthreads) {
+    if (order < TO_ORDER_ASCENDING || order > TO_ORDER_DEVICE) return -2;
+    if (s->integrator == TO_VERLET && !s->acc) return -3;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -314,7 +339,14 @@ int to_step(to_scene *s, int64_t nsteps, int order, int nthreads) {
         Fs = (double *)malloc((size_t)(ns > 0 ? ns : 1) * 3 * sizeof(double));
         if (!Fs) return -1;
     }
-    for (int64_t step = 0; step < nsteps; step++) {
+    double *bk = NULL;  /* RK2 backups: position and velocity per mass */
+    const int passes = s->integrator == TO_RK2 ? 2 : 1;
+    if (passes == 2) {
+        bk = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+        if (!bk) return -1;
+    }
+    for (int64_t pass = 0; pass < nsteps * passes; pass++) {
+        const int stage = (int)(pass % passes);
         if (order == TO_ORDER_ASCENDING) {
             for (int64_t j = 0; j < ns; j++) {
                 if (!spring_valid(s, j)) continue;
@@ -395,13 +427,13 @@ int to_step(to_scene *s, int64_t nsteps, int order, int nthreads) {
                     }
                 }
             }
-        } else {
-            return -2;
         }
         #pragma omp parallel for schedule(static) if (order == TO_ORDER_ATOMIC_OMP || order == TO_ORDER_DEVICE)
-        for (int64_t i = 0; i < n; i++) mass_update(s, i);
-        s->T_global = s->T_global + s->dt;
+        for (int64_t i = 0; i < n; i++)
+            mass_update(s, i, stage, bk ? bk + 6 * i : NULL, bk ? bk + 6 * i + 3 : NULL);
+        s->T_global = s->T_global + (passes == 2 ? 0.5 * s->dt : s->dt);
     }
+    free(bk);
     if (order == TO_ORDER_DEVICE) {
         free_incidence(&L);
         free(Fs);

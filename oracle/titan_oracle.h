@@ -76,11 +76,19 @@ typedef struct {
     double dt;
     double T_global;               /* host-accumulated simulation time           */
     int32_t heavy_threshold;       /* for TO_ORDER_DEVICE                        */
+    int32_t integrator;            /* TO_EULER (default), TO_VERLET, TO_RK2      */
 } to_scene;
 
+/* Integrators of massForcesAndUpdate (src/sim.cu:1141-1166): the default
+ * symplectic Euler, and the compile-time VERLET and RK2 variants.  VERLET
+ * keeps the acceleration as state (acc must not be NULL); RK2 evaluates the
+ * spring forces twice per step, at T and at T + dt/2 (src/sim.cu:1572-1583). */
+enum { TO_EULER = 0, TO_VERLET = 1, TO_RK2 = 2 };
+
 /* One time step == computeSpringForces (src/sim.cu:1046-1080) followed by
- * massForcesAndUpdate (src/sim.cu:1093-1169, CONSTRAINTS on, Euler) and the
- * host time update T += dt (src/sim.cu:1590).  Returns 0 on success. */
+ * massForcesAndUpdate (src/sim.cu:1093-1169, CONSTRAINTS on) and the host
+ * time update T += dt (src/sim.cu:1590); with RK2 both twice, T += dt/2
+ * after each (src/sim.cu:1572-1583).  Returns 0 on success. */
 int to_step(to_scene *s, int64_t nsteps, int order, int nthreads);
 
 /* Spring force on the RIGHT endpoint (src/sim.cu:1054-1065); the left one gets

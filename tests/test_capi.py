@@ -336,3 +336,13 @@ def test_export_indices_on_host_before_start():
     assert (idx[:-2, 0] == sc["left"][:-2]).all() and (idx[:-2, 1] == sc["right"][:-2]).all()
     assert (idx[-2:] == 0).all()  # detached springs export (0, 0)
     s.close()
+
+
+def test_set_integrator_validates():
+    s = tg.Sim(tg.FP64)
+    for v in (-1, 3):
+        with pytest.raises(tg.TitanError, match="EINVAL"):
+            s.set_integrator(v)
+    s.set_integrator(tg.RK2)
+    s.set_integrator(tg.VERLET)
+    s.close()

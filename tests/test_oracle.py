@@ -276,3 +276,39 @@ def test_heavy_order_close_to_ascending():
     a.step(1, po.ASCENDING)
     b.step(1, po.DEVICE)
     assert np.max(np.abs(a.vel - b.vel)) <= 1e-12 * np.max(np.abs(a.vel))
+
+
+def test_integrator_free_fall_known_answers():
+    """Constant gravity, no springs: the reference's VERLET starts with a = 0,
+    which makes its positions the discrete Euler sum z0 - g dt^2 n(n+1)/2;
+    its RK2 (half step, then full step from the saved state) integrates a
+    constant acceleration exactly: z0 - g (n dt)^2 / 2."""
+    n_steps, dt, g = 2000, 1e-4, 9.81
+    sc = {"pos": np.array([[0.0, 0.0, 10.0], [1.0, 2.0, 3.0]]), "m": np.array([0.1, 0.2]),
+          "left": np.zeros(0, np.int32), "right": np.zeros(0, np.int32), "k": np.zeros(0), "rest": np.zeros(0),
+          "planes": [], "balls": [], "g": np.array([0.0, 0.0, -g]), "dt": dt}
+    for integ, want in ((1, lambda z0, n: z0 - g * dt * dt * n * (n + 1) / 2),
+                        (2, lambda z0, n: z0 - 0.5 * g * (n * dt) ** 2)):
+        o = po.OracleSim(dict(sc, integrator=integ))
+        o.step(n_steps)
+        for i, z0 in ((0, 10.0), (1, 3.0)):
+            assert abs(o.pos[i, 2] - want(z0, n_steps)) < 1e-12
+        assert np.array_equal(o.pos[:, :2], sc["pos"][:, :2])
+        assert abs(o.time - n_steps * dt) < 1e-12
+
+
+def test_integrators_agree_on_a_smooth_oscillation():
+    """A stiff pair of masses: the three integrators are first/second order
+    schemes of the same ODE and agree to O(dt) over one period."""
+    rng = np.random.default_rng(2)
+    from titan_gb300 import workloads as wl
+    sc = wl.lattice_scene((0, 0, 5.0), (0.5, 0.5, 0.5), 3, 3, 3, k=2e3, damping=0.0)
+    sc["g"] = np.zeros(3)
+    sc["vel"] = rng.normal(scale=0.05, size=sc["pos"].shape)
+    pos = []
+    for integ in (0, 1, 2):
+        o = po.OracleSim(dict(sc, integrator=integ))
+        o.step(2000)
+        pos.append(o.pos.copy())
+    assert np.max(np.abs(pos[1] - pos[0])) < 2e-3
+    assert np.max(np.abs(pos[2] - pos[0])) < 2e-3

@@ -20,6 +20,7 @@ __all__ = ["FP64", "FP32", "FP32C", "TitanError", "Sim", "lattice", "lattice_spr
            "library_path"]
 
 FP64, FP32, FP32C = 0, 1, 2
+EULER, VERLET, RK2 = 0, 1, 2
 PRECISION_NAMES = {FP64: "f64", FP32: "f32", FP32C: "f32c"}
 
 _ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ELIMIT", 5: "ESTATE", 6: "ETIMEOUT", 7: "EBUDGET"}
@@ -54,6 +55,7 @@ _SIGS = {
     "titan_gb300_add_ball": (ctypes.c_int, [_P, _D, ctypes.c_double]),
     "titan_gb300_clear_constraints": (ctypes.c_int, [_P]),
     "titan_gb300_set_time_step": (ctypes.c_int, [_P, ctypes.c_double]),
+    "titan_gb300_set_integrator": (ctypes.c_int, [_P, ctypes.c_int]),
     "titan_gb300_get_time_step": (ctypes.c_double, [_P]),
     "titan_gb300_set_global_acc": (ctypes.c_int, [_P, _D]),
     "titan_gb300_set_bodies": (ctypes.c_int, [_P, ctypes.c_int64, _I64]),
@@ -243,6 +245,10 @@ class Sim:
 
     def device_bytes(self) -> int:
         return int(self._L.titan_gb300_device_bytes(self._h))
+
+    def set_integrator(self, kind: int):
+        """0 symplectic Euler (default), 1 Verlet, 2 RK2."""
+        self._check(self._L.titan_gb300_set_integrator(self._h, int(kind)), "set_integrator")
 
     def set_time_step(self, dt):
         self._check(self._L.titan_gb300_set_time_step(self._h, dt), "set_time_step")

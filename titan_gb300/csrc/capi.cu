@@ -89,7 +89,14 @@ struct titan_gb300_sim {
     int parity = 0;
     std::vector<double> mT0;       // per-mass local time at its last upload
     std::vector<int64_t> mTstep;   // step count at that upload
-    std::vector<std::pair<int64_t, double>> dt_log;  // (first step, dt)
+    struct DtSeg {
+        int64_t first;  // first step of the segment
+        double dt;
+        int halves;     // 2: RK2 advances time by dt/2 twice per step
+    };
+    std::vector<DtSeg> dt_log;
+    int integrator = tg::INTEG_EULER;
+    int passes() const { return integrator == tg::INTEG_RK2 ? 2 : 1; }
 
     // device
     tg::Plan plan;
@@ -135,8 +142,9 @@ struct titan_gb300_sim {
     bool plan_adopted = false;
     int plan_tile = 0;  // tile size the current plan was built with
 
-    cudaError_t launch(int parity, int write_acc) {
+    cudaError_t launch(int parity, int write_acc, int stage = 0) {
         if (args.ntiles == 0) return cudaSuccess;
+        args.rk2_stage = stage;
         if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
         if (use_ws) return tg::launch_step_ws(prec, args, ctas, ws_warps, parity, write_acc, stream);
         if (use_async)
@@ -197,6 +205,10 @@ void fill_params(titan_gb300_sim *s) {
     p.dt = s->dt;
     p.dt_hi = (float)s->dt;
     p.dt_lo = (float)(s->dt - (double)p.dt_hi);
+    p.integrator = s->integrator;
+    p.dt2 = std::pow(s->dt, 2);
+    p.dt2f = (float)p.dt2;
+    p.launch_dt = s->integrator == tg::INTEG_RK2 ? 0.5 * s->dt : s->dt;
     for (int c = 0; c < 3; c++) {
         p.g[c] = s->g[c];
         p.gf[c] = (float)s->g[c];
@@ -474,7 +486,7 @@ int build_device(titan_gb300_sim *s) {
     s->rplan = tg::ResPlan();
     s->rargs = tg::ResArgs{};
     {
-        const int cap = resident_cap(s);
+        const int cap = s->integrator == tg::INTEG_EULER ? resident_cap(s) : 0;
         if (cap > 0) {
             tg::build_resident(in, P, cap, cap, s->rplan);
             if (s->rplan.nbins > 0) {
@@ -733,7 +745,15 @@ void mass_times(titan_gb300_sim *s, const int64_t *idx, int64_t count, double *T
         for (size_t r = 0; r < s->dt_log.size(); r++) {
             int64_t b = s->dt_log[r].first;
             int64_t e = r + 1 < s->dt_log.size() ? s->dt_log[r + 1].first : s->steps;
-            double d = s->dt_log[r].second;
+            double d = s->dt_log[r].dt;
+            if (s->dt_log[r].halves == 2) {  // RK2: mass.T += 0.5 * dt twice per step
+                const double h = 0.5 * d;
+                for (int64_t z = std::max(b, st); z < e; z++) {
+                    t = t + h;
+                    t = t + h;
+                }
+                continue;
+            }
             for (int64_t z = std::max(b, st); z < e; z++) t = t + d;
         }
         memo[key] = t;
@@ -749,10 +769,11 @@ cudaGraphExec_t get_graph(titan_gb300_sim *s, int len, int parity, cudaError_t &
     e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return nullptr;
     int p = parity;
-    for (int i = 0; i < len; i++) {
-        s->launch(p, 0);
-        p ^= 1;
-    }
+    for (int i = 0; i < len; i++)
+        for (int q = 0; q < s->passes(); q++) {
+            s->launch(p, 0, q);
+            p ^= 1;
+        }
     e = cudaStreamEndCapture(s->stream, &g);
     if (e != cudaSuccess) return nullptr;
     cudaGraphExec_t ex = nullptr;
@@ -1057,12 +1078,35 @@ int titan_gb300_clear_constraints(titan_gb300_sim *s) {
     return TITAN_GB300_OK;
 }
 
+int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (kind < tg::INTEG_EULER || kind > tg::INTEG_RK2)
+        return s->fail(TITAN_GB300_EINVAL, "integrator must be 0 (Euler), 1 (Verlet) or 2 (RK2)");
+    if (kind == s->integrator) return TITAN_GB300_OK;
+    if (!s->started) {
+        s->integrator = kind;
+        return TITAN_GB300_OK;
+    }
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    CK(cudaStreamSynchronize(s->stream), "set integrator");
+    const bool was_res = s->use_res;
+    s->integrator = kind;
+    s->dt_log.push_back({s->steps, s->dt, s->passes()});
+    s->drop_graphs();
+    if (was_res) {  // resident bins run Euler only: rebuild without them
+        int rc = pull_state(s);
+        if (rc) return rc;
+        return build_device(s);
+    }
+    return upload_params(s);
+}
+
 int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) {
     if (!s) return TITAN_GB300_EINVAL;
     if (!(dt > 0)) return s->fail(TITAN_GB300_EINVAL, "Cannot set time step to negative or zero value.");
     s->dt = dt;
     if (s->started) {
-        s->dt_log.emplace_back(s->steps, dt);
+        s->dt_log.push_back({s->steps, dt, s->passes()});
         return upload_params(s);
     }
     return TITAN_GB300_OK;
@@ -1113,7 +1157,7 @@ int titan_gb300_start(titan_gb300_sim *s, int tile_masses) {
     s->tile_masses = tile_masses;
     s->T = 0.0;
     s->steps = 0;
-    s->dt_log.assign(1, {0, s->dt});
+    s->dt_log.assign(1, {0, s->dt, s->passes()});
     s->mT0.assign(s->n, 0.0);
     s->mTstep.assign(s->n, 0);
     int rc = build_device(s);
@@ -1139,19 +1183,29 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
         s->steps += nsteps;
         return TITAN_GB300_OK;
     }
+    const int P = s->passes();
     int64_t rem = nsteps - 1;
     while (rem > 0) {
         int len = (int)std::min<int64_t>(rem, kChunk);
         cudaGraphExec_t g = get_graph(s, len, s->parity, e);
         if (!g) return s->cuda_fail(e, "build step graph");
         CK(cudaGraphLaunch(g, s->stream), "launch step graph");
-        s->parity ^= (len & 1);
+        s->parity ^= ((len * P) & 1);
         rem -= len;
     }
-    CK(s->launch(s->parity, 1),
-       "launch step");
-    s->parity ^= 1;
-    for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
+    for (int q = 0; q < P; q++) {  // the last step also writes the accelerations
+        CK(s->launch(s->parity, q == P - 1, q), "launch step");
+        s->parity ^= 1;
+    }
+    if (P == 2) {
+        const double h = 0.5 * s->dt;
+        for (int64_t i = 0; i < nsteps; i++) {  // src/sim.cu:1574-1583
+            s->T = s->T + h;
+            s->T = s->T + h;
+        }
+    } else {
+        for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
+    }
     s->steps += nsteps;
     return TITAN_GB300_OK;
 }

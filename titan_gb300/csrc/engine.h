@@ -61,6 +61,8 @@ struct WsLayout {
 constexpr int kWsMaxStages = 3;
 constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
 
+enum { INTEG_EULER = 0, INTEG_VERLET = 1, INTEG_RK2 = 2 };
+
 struct DevParams {
     double dt;
     double g[3];
@@ -72,6 +74,11 @@ struct DevParams {
     float pad;
     float planef[kMaxPlanes][6];
     float ballf[kMaxBalls][4];
+    int32_t integrator;           // INTEG_*
+    float dt2f;                   // (float) pow(dt, 2)
+    double dt2;                   // pow(dt, 2), computed on the host as the reference's Vec code does
+    double launch_dt;             // time advanced by one launch: dt, or dt / 2 for RK2
+    double pad2;
 };
 
 static_assert(sizeof(DevParams) % 16 == 0, "DevParams is copied as 16-byte vectors");
@@ -104,6 +111,7 @@ struct StepArgs {
     int64_t npad;
     int32_t slots, ecap, hcap;
     int32_t ntiles;
+    int32_t rk2_stage;         // RK2: 0 first half step, 1 second (launches alternate)
     int *err;                  // set by a kernel whose bounded wait gave up
     PipeLayout pipe;
     WsLayout ws;

@@ -12,6 +12,18 @@
 namespace tg {
 namespace {
 
+// (hi, lo) += (wh + wl) * (dt_hi + dt_lo) + extra, compensated: the product's
+// rounding error and the low parts are carried into lo.
+__device__ __forceinline__ void comp_add_prod(float &hi, float &lo, float wh, float wl, float dt_hi, float dt_lo,
+                                              float extra) {
+    const float q = wh * dt_hi;
+    const float qe = fmaf(wh, dt_hi, -q) + fmaf(wh, dt_lo, wl * dt_hi) + extra;
+    float sum, err;
+    two_sum(hi, q, sum, err);
+    err += lo + qe;
+    fast_two_sum(sum, err, hi, lo);
+}
+
 template <int PREC>
 __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti, int64_t g, uint8_t fl,
                                           typename Real<PREC>::T m, typename Real<PREC>::T F0,
@@ -50,14 +62,38 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
         }
         const double dt = prm->dt;
         double acc[3] = {Fd[0] / m, Fd[1] / m, Fd[2] / m};
+        double *ac = reinterpret_cast<double *>(a.acc);
+        if (prm->integrator == INTEG_VERLET) {  // src/sim.cu:1155-1159; acc is state
+            double ap[3] = {ac[g], ac[np + g], ac[2 * np + g]};
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            s.v[c] = s.v[c] + acc[c] * dt;
-            s.x[c] = s.x[c] + s.v[c] * dt;
+            for (int c = 0; c < 3; c++) s.v[c] = s.v[c] + (0.5 * (ap[c] + acc[c])) * dt;
+#pragma unroll
+            for (int c = 0; c < 3; c++) s.x[c] = s.x[c] + (s.v[c] * dt + (0.5 * acc[c]) * prm->dt2);
+            write_acc = 1;
+        } else if (prm->integrator == INTEG_RK2) {  // src/sim.cu:1141-1154
+            if (a.rk2_stage == 0) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) s.x[c] = s.x[c] + (0.5 * s.v[c]) * dt;
+#pragma unroll
+                for (int c = 0; c < 3; c++) s.v[c] = s.v[c] + (0.5 * acc[c]) * dt;
+            } else {
+                // the step's starting state is still this mass's record in
+                // the buffer this launch writes
+                const St<PREC> b = load_state<PREC>(out, gs);
+#pragma unroll
+                for (int c = 0; c < 3; c++) s.x[c] = b.x[c] + s.v[c] * dt;
+#pragma unroll
+                for (int c = 0; c < 3; c++) s.v[c] = b.v[c] + acc[c] * dt;
+            }
+        } else {  // symplectic Euler, src/sim.cu:1161-1166
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                s.v[c] = s.v[c] + acc[c] * dt;
+                s.x[c] = s.x[c] + s.v[c] * dt;
+            }
         }
         store_state<PREC>(out, gs, s);
         if (write_acc) {
-            double *ac = reinterpret_cast<double *>(a.acc);
             ac[g] = acc[0];
             ac[np + g] = acc[1];
             ac[2 * np + g] = acc[2];
@@ -112,31 +148,83 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
         }
         const float inv_m = __frcp_rn(m);
         float acc[3];
+        float *ac = reinterpret_cast<float *>(a.acc);
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            acc[c] = Ff[c] * inv_m;
-            if constexpr (PREC == P_FP32C) {
-                // v += a dt with dt = dt_hi + dt_lo, compensated
-                float p = acc[c] * prm->dt_hi;
-                float pe = fmaf(acc[c], prm->dt_hi, -p) + acc[c] * prm->dt_lo;
-                float sum, err;
-                two_sum(s.v[c], p, sum, err);
-                err += s.vl[c] + pe;
-                fast_two_sum(sum, err, s.v[c], s.vl[c]);
-                // x += v dt
-                float q = s.v[c] * prm->dt_hi;
-                float qe = fmaf(s.v[c], prm->dt_hi, -q) + fmaf(s.v[c], prm->dt_lo, s.vl[c] * prm->dt_hi);
-                two_sum(s.x[c], q, sum, err);
-                err += s.xl[c] + qe;
-                fast_two_sum(sum, err, s.x[c], s.xl[c]);
+        for (int c = 0; c < 3; c++) acc[c] = Ff[c] * inv_m;
+        if (prm->integrator == INTEG_VERLET) {
+            // v += (a_prev + a) dt / 2;  x += v dt + a dt^2 / 2
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float w = 0.5f * (ac[(int64_t)c * np + g] + acc[c]);
+                const float r = (0.5f * acc[c]) * prm->dt2f;
+                if constexpr (PREC == P_FP32C) {
+                    comp_add_prod(s.v[c], s.vl[c], w, 0.f, prm->dt_hi, prm->dt_lo, 0.f);
+                    comp_add_prod(s.x[c], s.xl[c], s.v[c], s.vl[c], prm->dt_hi, prm->dt_lo, r);
+                } else {
+                    s.v[c] = s.v[c] + w * prm->dt_hi;
+                    s.x[c] = s.x[c] + (s.v[c] * prm->dt_hi + r);
+                }
+            }
+            write_acc = 1;
+        } else if (prm->integrator == INTEG_RK2) {
+            if (a.rk2_stage == 0) {
+                // x += v dt / 2 (with the step's starting v);  v += a dt / 2
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    if constexpr (PREC == P_FP32C) {
+                        const float vh = s.v[c], vlo = s.vl[c];
+                        comp_add_prod(s.x[c], s.xl[c], 0.5f * vh, 0.5f * vlo, prm->dt_hi, prm->dt_lo, 0.f);
+                        comp_add_prod(s.v[c], s.vl[c], 0.5f * acc[c], 0.f, prm->dt_hi, prm->dt_lo, 0.f);
+                    } else {
+                        s.x[c] = s.x[c] + (0.5f * s.v[c]) * prm->dt_hi;
+                        s.v[c] = s.v[c] + (0.5f * acc[c]) * prm->dt_hi;
+                    }
+                }
             } else {
-                s.v[c] = s.v[c] + acc[c] * prm->dt_hi;
-                s.x[c] = s.x[c] + s.v[c] * prm->dt_hi;
+                // from the step's starting state, still this mass's record in
+                // the buffer this launch writes: x = x0 + v dt;  v = v0 + a dt
+                const St<PREC> b = load_state<PREC>(out, gs);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    if constexpr (PREC == P_FP32C) {
+                        const float vh = s.v[c], vlo = s.vl[c];
+                        s.x[c] = b.x[c];
+                        s.xl[c] = b.xl[c];
+                        comp_add_prod(s.x[c], s.xl[c], vh, vlo, prm->dt_hi, prm->dt_lo, 0.f);
+                        s.v[c] = b.v[c];
+                        s.vl[c] = b.vl[c];
+                        comp_add_prod(s.v[c], s.vl[c], acc[c], 0.f, prm->dt_hi, prm->dt_lo, 0.f);
+                    } else {
+                        s.x[c] = b.x[c] + s.v[c] * prm->dt_hi;
+                        s.v[c] = b.v[c] + acc[c] * prm->dt_hi;
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if constexpr (PREC == P_FP32C) {
+                    // v += a dt with dt = dt_hi + dt_lo, compensated
+                    float p = acc[c] * prm->dt_hi;
+                    float pe = fmaf(acc[c], prm->dt_hi, -p) + acc[c] * prm->dt_lo;
+                    float sum, err;
+                    two_sum(s.v[c], p, sum, err);
+                    err += s.vl[c] + pe;
+                    fast_two_sum(sum, err, s.v[c], s.vl[c]);
+                    // x += v dt
+                    float q = s.v[c] * prm->dt_hi;
+                    float qe = fmaf(s.v[c], prm->dt_hi, -q) + fmaf(s.v[c], prm->dt_lo, s.vl[c] * prm->dt_hi);
+                    two_sum(s.x[c], q, sum, err);
+                    err += s.xl[c] + qe;
+                    fast_two_sum(sum, err, s.x[c], s.xl[c]);
+                } else {
+                    s.v[c] = s.v[c] + acc[c] * prm->dt_hi;
+                    s.x[c] = s.x[c] + s.v[c] * prm->dt_hi;
+                }
             }
         }
         store_state<PREC>(out, gs, s);
         if (write_acc) {
-            float *ac = reinterpret_cast<float *>(a.acc);
             ac[g] = acc[0];
             ac[np + g] = acc[1];
             ac[2 * np + g] = acc[2];

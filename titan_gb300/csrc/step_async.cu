@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(512) k_step_async(StepArgs a, int parity, int 
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
     const StepTime t = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->launch_dt;
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
     const StepTime t = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->launch_dt;
 
     // phase-C inputs of this thread's own mass, issued first
     const int i_own = threadIdx.x;

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(512) k_step_pipe(StepArgs a, int parity, int w
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
     const StepTime tm = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + prm->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + prm->launch_dt;
     const int ntiles = a.ntiles;
     const int t0 = blockIdx.x;
     if (t0 >= ntiles) return;

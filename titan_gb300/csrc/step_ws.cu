@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
     for (int q = threadIdx.x; q < (int)(sizeof(DevParams) / 16); q += blockDim.x)
         reinterpret_cast<int4 *>(prm)[q] = __ldg(reinterpret_cast<const int4 *>(a.prm) + q);
     const StepTime tm = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + a.prm->dt;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + a.prm->launch_dt;
     const int ncw = (int)(blockDim.x >> 5) - 1;  // consumer warps (even)
     const int gw = ncw >> 1;                     // warps per group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

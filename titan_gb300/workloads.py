@@ -158,6 +158,8 @@ def load(sim: Sim, sc: dict, start=True, tile_masses=0, threads=0, kernel=0, res
     the default, else (mode, bin_masses, threads) for set_resident."""
     sim.set_time_step(sc["dt"])
     sim.set_global_acc(sc["g"])
+    if sc.get("integrator", 0):
+        sim.set_integrator(sc["integrator"])
     sim.set_masses(sc["pos"], sc["m"], vel=sc.get("vel"), ext=sc.get("ext"), fixed=sc.get("fixed"),
                    drag=sc.get("drag"))
     sim.set_springs(sc["left"], sc["right"], sc["k"], sc["rest"], damping=sc.get("damping"),
