@@ -146,11 +146,11 @@ struct titan_gb300_sim {
         if (args.ntiles == 0) return cudaSuccess;
         args.rk2_stage = stage;
         if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
-        if (use_ws) return tg::launch_step_ws(prec, args, ctas, ws_warps, parity, write_acc, stream);
+        if (use_ws) return tg::launch_step_ws(prec, integrator, args, ctas, ws_warps, parity, write_acc, stream);
         if (use_async)
             return tg::launch_step_async(prec, args, (int)args.ntiles, threads, smem, parity, write_acc, stream);
-        return tg::launch_step(prec, step_variant, args, (int)args.ntiles, threads, smem, parity, write_acc,
-                               stream);
+        return tg::launch_step(prec, step_variant, integrator, args, (int)args.ntiles, threads, smem, parity,
+                               write_acc, stream);
     }
 
     int fail(int code, const std::string &msg) {
@@ -575,7 +575,7 @@ int build_device(titan_gb300_sim *s) {
         W.total = W.mbar + (2 * W.nstages + 2) * 8 + 32;
         s->ws_warps = s->threads_req > 0 ? s->threads_req / 32 : tg::kWsMaxConsumerWarps;
         s->ws_warps = std::max(2, std::min(tg::kWsMaxConsumerWarps, s->ws_warps)) & ~1;
-        CK(tg::step_ws_prepare(s->prec, (size_t)W.total), "set shared memory");
+        CK(tg::step_ws_prepare(s->prec, s->integrator, (size_t)W.total), "set shared memory");
         int sms = 0, dev = 0;
         CK(cudaGetDevice(&dev), "device");
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
@@ -608,7 +608,7 @@ int build_device(titan_gb300_sim *s) {
         if (s->use_async)
             CK(tg::step_async_prepare(s->prec, s->smem), "set shared memory");
         else
-            CK(tg::step_prepare(s->prec, s->step_variant, s->smem), "set shared memory");
+            CK(tg::step_prepare(s->prec, s->step_variant, s->integrator, s->smem), "set shared memory");
     }
     a.ntiles = (int32_t)tiles_run.size();
     if (P.ent_ends.size() > (size_t)INT32_MAX || P.halo.size() > (size_t)INT32_MAX)
@@ -1098,6 +1098,11 @@ int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) {
         if (rc) return rc;
         return build_device(s);
     }
+    // the kernels of the new integrator need their shared-memory limit
+    if (s->use_ws)
+        CK(tg::step_ws_prepare(s->prec, kind, (size_t)s->args.ws.total), "set shared memory");
+    else if (!s->use_pipe && !s->use_async)
+        CK(tg::step_prepare(s->prec, s->step_variant, kind, s->smem), "set shared memory");
     return upload_params(s);
 }
 

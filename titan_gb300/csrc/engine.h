@@ -179,9 +179,9 @@ size_t tile_smem_bytes(int precision, int slots, int entries, int heavy);
 // threads per CTA, registers capped for 3 or 4 resident CTAs per SM.
 constexpr int kStepVariants = 3;
 const void *step_kernel_capped(int precision, int variant);  // null if not compiled
-cudaError_t step_prepare(int precision, int variant, size_t smem);
-cudaError_t launch_step(int precision, int variant, const StepArgs &a, int ntiles, int threads, size_t smem,
-                        int parity, int write_acc, cudaStream_t s);
+cudaError_t step_prepare(int precision, int variant, int integ, size_t smem);
+cudaError_t launch_step(int precision, int variant, int integ, const StepArgs &a, int ntiles, int threads,
+                        size_t smem, int parity, int write_acc, cudaStream_t s);
 // Pipelined persistent variant (step_tma.cu): grid of `ctas` CTAs walking the
 // tiles, TMA bulk copies of the next tile overlapping the current tile.
 cudaError_t step_pipe_prepare(int precision, size_t smem);
@@ -197,8 +197,8 @@ cudaError_t launch_step_async(int precision, const StepArgs &a, int ntiles, int 
 // Warp-specialised persistent kernel (step_ws.cu): `ctas` CTAs of
 // consumer_warps + 1 warps; the last warp streams tiles into a ring of
 // stages, the others compute.
-cudaError_t step_ws_prepare(int precision, size_t smem);
-cudaError_t launch_step_ws(int precision, const StepArgs &a, int ctas, int consumer_warps, int parity,
+cudaError_t step_ws_prepare(int precision, int integ, size_t smem);
+cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas, int consumer_warps, int parity,
                            int write_acc, cudaStream_t s);
 // bytes of one state record / one slab entry record for a precision
 int state_record_bytes(int precision);

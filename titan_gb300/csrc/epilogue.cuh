@@ -24,7 +24,9 @@ __device__ __forceinline__ void comp_add_prod(float &hi, float &lo, float wh, fl
     fast_two_sum(sum, err, hi, lo);
 }
 
-template <int PREC>
+// INTEG: the integrator (INTEG_*) fixed at compile time, or -1 to read it
+// from prm at run time.
+template <int PREC, int INTEG = -1>
 __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti, int64_t g, uint8_t fl,
                                           typename Real<PREC>::T m, typename Real<PREC>::T F0,
                                           typename Real<PREC>::T F1, typename Real<PREC>::T F2, St<PREC> &s,
@@ -63,14 +65,15 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
         const double dt = prm->dt;
         double acc[3] = {Fd[0] / m, Fd[1] / m, Fd[2] / m};
         double *ac = reinterpret_cast<double *>(a.acc);
-        if (prm->integrator == INTEG_VERLET) {  // src/sim.cu:1155-1159; acc is state
+        const int integ = INTEG >= 0 ? INTEG : prm->integrator;
+        if (integ == INTEG_VERLET) {  // src/sim.cu:1155-1159; acc is state
             double ap[3] = {ac[g], ac[np + g], ac[2 * np + g]};
 #pragma unroll
             for (int c = 0; c < 3; c++) s.v[c] = s.v[c] + (0.5 * (ap[c] + acc[c])) * dt;
 #pragma unroll
             for (int c = 0; c < 3; c++) s.x[c] = s.x[c] + (s.v[c] * dt + (0.5 * acc[c]) * prm->dt2);
             write_acc = 1;
-        } else if (prm->integrator == INTEG_RK2) {  // src/sim.cu:1141-1154
+        } else if (integ == INTEG_RK2) {  // src/sim.cu:1141-1154
             if (a.rk2_stage == 0) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) s.x[c] = s.x[c] + (0.5 * s.v[c]) * dt;
@@ -151,7 +154,8 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
         float *ac = reinterpret_cast<float *>(a.acc);
 #pragma unroll
         for (int c = 0; c < 3; c++) acc[c] = Ff[c] * inv_m;
-        if (prm->integrator == INTEG_VERLET) {
+        const int integ = INTEG >= 0 ? INTEG : prm->integrator;
+        if (integ == INTEG_VERLET) {
             // v += (a_prev + a) dt / 2;  x += v dt + a dt^2 / 2
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -166,7 +170,7 @@ __device__ __forceinline__ void integrate(const StepArgs &a, const TileInfo &ti,
                 }
             }
             write_acc = 1;
-        } else if (prm->integrator == INTEG_RK2) {
+        } else if (integ == INTEG_RK2) {
             if (a.rk2_stage == 0) {
                 // x += v dt / 2 (with the step's starting v);  v += a dt / 2
 #pragma unroll

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(512) k_resident(StepArgs a, ResArgs r, int par
                 TileInfo tb{};
                 tb.body = bd[k];
                 St<PREC> s = load_state_smem<PREC>(cur, i);
-                integrate<PREC>(a, tb, g[k], fl[k], mm[k], F0, F1, F2, s, nxt, i, last, np, prm);
+                integrate<PREC, INTEG_EULER>(a, tb, g[k], fl[k], mm[k], F0, F1, F2, s, nxt, i, last, np, prm);
             }
             __syncthreads();
             T = T + dt;

@@ -33,23 +33,34 @@ size_t tile_smem_bytes(int precision, int slots, int entries, int heavy) {
     return (size_t)(align16((int64_t)slots * rec) + (int64_t)entries * slot + 3 * (int64_t)heavy * rs);
 }
 
-const void *step_kernel(int precision, int variant) {
-    if (variant != 0 && precision != P_FP64) return step_kernel_capped(precision, variant);
-    return precision == P_FP64   ? (const void *)k_step<P_FP64, 512, 1>
-           : precision == P_FP32 ? (const void *)k_step<P_FP32, 512, 1>
-                                 : (const void *)k_step<P_FP32C, 512, 1>;
+template <int PREC>
+const void *step_kernel_default(int integ) {
+    switch (integ) {
+        case INTEG_VERLET: return (const void *)k_step<PREC, 512, 1, INTEG_VERLET>;
+        case INTEG_RK2: return (const void *)k_step<PREC, 512, 1, INTEG_RK2>;
+        default: return (const void *)k_step<PREC, 512, 1, INTEG_EULER>;
+    }
 }
 
-cudaError_t step_prepare(int precision, int variant, size_t smem) {
-    const void *f = step_kernel(precision, variant);
+// The register-capped variants exist for Euler in the FP32 forms; other
+// requests run the default launch bounds.
+const void *step_kernel(int precision, int variant, int integ) {
+    if (variant != 0 && precision != P_FP64 && integ == INTEG_EULER) return step_kernel_capped(precision, variant);
+    return precision == P_FP64   ? step_kernel_default<P_FP64>(integ)
+           : precision == P_FP32 ? step_kernel_default<P_FP32>(integ)
+                                 : step_kernel_default<P_FP32C>(integ);
+}
+
+cudaError_t step_prepare(int precision, int variant, int integ, size_t smem) {
+    const void *f = step_kernel(precision, variant, integ);
     if (!f) return cudaErrorInvalidValue;
     return raise_smem_limit(f, smem);
 }
 
-cudaError_t launch_step(int precision, int variant, const StepArgs &a, int ntiles, int threads, size_t smem,
-                        int parity, int write_acc, cudaStream_t s) {
+cudaError_t launch_step(int precision, int variant, int integ, const StepArgs &a, int ntiles, int threads,
+                        size_t smem, int parity, int write_acc, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    const void *f = step_kernel(precision, variant);
+    const void *f = step_kernel(precision, variant, integ);
     if (!f) return cudaErrorInvalidValue;
     void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
     return cudaLaunchKernel(f, dim3(ntiles), dim3(threads), args, smem, s);

@@ -18,7 +18,8 @@
 //
 // LBT / LBM are the kernel's launch bounds (threads per CTA, minimum CTAs
 // per SM): they cap registers per thread at 65536 / (LBT * LBM), trading
-// registers for resident warps.
+// registers for resident warps.  INTEG is the integrator (INTEG_*), fixed at
+// compile time so that each instance carries only its own update.
 #pragma once
 
 #include <cstdint>
@@ -57,7 +58,7 @@ __device__ __forceinline__ void copy_record(uint8_t *dst, const uint8_t *src) {
         reinterpret_cast<float4 *>(dst)[v] = __ldg(reinterpret_cast<const float4 *>(src) + v);
 }
 
-template <int PREC, int LBT, int LBM>
+template <int PREC, int LBT, int LBM, int INTEG>
 __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int write_acc) {
     using R = typename Real<PREC>::T;
     constexpr int kRec = rec_bytes<PREC>();
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
             }
         }
         St<PREC> s = load_state_smem<PREC>(st, i);
-        integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, s, out, g, write_acc, np, prm);
+        integrate<PREC, INTEG>(a, ti, g, fl, m, F0, F1, F2, s, out, g, write_acc, np, prm);
     }
 }
 

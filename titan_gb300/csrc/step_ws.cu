@@ -76,7 +76,7 @@ __device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile
     return false;
 }
 
-template <int PREC>
+template <int PREC, int INTEG>
 __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parity, int write_acc) {
     using R = typename Real<PREC>::T;
     constexpr int kRec = ws_rec<PREC>();
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                     for (uint32_t w = 0; w < nw; w++) gather_word<PREC>(slots, ip[32 * w], w, d, F0, F1, F2);
                 }
                 St<PREC> sv = load_state_smem<PREC>(st, i);
-                integrate<PREC>(a, ti, g, fl, m, F0, F1, F2, sv, out, g, write_acc, np, prm);
+                integrate<PREC, INTEG>(a, ti, g, fl, m, F0, F1, F2, sv, out, g, write_acc, np, prm);
             }
             // the stage is free once every warp of the group is past it; order
             // this thread's slot writes before the copies that will reuse it
@@ -300,27 +300,33 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
 }
 
 template <int PREC>
-const void *ws_kernel() {
-    return (const void *)k_step_ws<PREC>;
+const void *ws_kernel(int integ) {
+    switch (integ) {
+        case INTEG_VERLET: return (const void *)k_step_ws<PREC, INTEG_VERLET>;
+        case INTEG_RK2: return (const void *)k_step_ws<PREC, INTEG_RK2>;
+        default: return (const void *)k_step_ws<PREC, INTEG_EULER>;
+    }
 }
 
-const void *ws_kernel(int precision) {
-    return precision == P_FP64 ? ws_kernel<P_FP64>() : precision == P_FP32 ? ws_kernel<P_FP32>() : ws_kernel<P_FP32C>();
+const void *ws_kernel(int precision, int integ) {
+    return precision == P_FP64   ? ws_kernel<P_FP64>(integ)
+           : precision == P_FP32 ? ws_kernel<P_FP32>(integ)
+                                 : ws_kernel<P_FP32C>(integ);
 }
 
 }  // namespace
 
-cudaError_t step_ws_prepare(int precision, size_t smem) {
-    return raise_smem_limit(ws_kernel(precision), smem);
+cudaError_t step_ws_prepare(int precision, int integ, size_t smem) {
+    return raise_smem_limit(ws_kernel(precision, integ), smem);
 }
 
-cudaError_t launch_step_ws(int precision, const StepArgs &a, int ctas, int consumer_warps, int parity,
+cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas, int consumer_warps, int parity,
                            int write_acc, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (consumer_warps < 2 || consumer_warps > kWsMaxConsumerWarps || (consumer_warps & 1))
         return cudaErrorInvalidValue;
     void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
-    return cudaLaunchKernel(ws_kernel(precision), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
+    return cudaLaunchKernel(ws_kernel(precision, integ), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
                             (size_t)a.ws.total, s);
 }
 
