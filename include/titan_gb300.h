@@ -355,6 +355,16 @@ int64_t titan_gb300_plan_table(const titan_gb300_sim *sim, int table, void *out)
 /* Lattice builder of createLattice (src/sim.cu:1923-1944, src/object.cu:232-293):
  * fills pos (3*nx*ny*nz) and, when non-NULL, left/right/rest of the
  * titan_gb300_lattice_springs(nx,ny,nz) springs, in the reference's order. */
+/* Point-in-mesh test of STL import on GPU `device` (stl::stlFile::inside,
+ * include/Titan/stlparser.h:213-276, for Simulation::importFromSTL,
+ * src/sim.cu:1855-1921): inside[i] = 1 when more than half of num_rays rays
+ * from point i cross the triangles an odd number of times.  Rays come from a
+ * counter-based generator keyed by seed, point and ray (the reference uses
+ * rand()), so the result is reproducible.  tri: 9 doubles per triangle
+ * (v1, v2, v3); pts: 3 per point; num_rays in [1, 64].  Blocking. */
+int titan_gb300_stl_inside(int device, const double *tri, int64_t ntri, const double *pts, int64_t npts,
+                           int num_rays, uint64_t seed, uint8_t *inside);
+
 int64_t titan_gb300_lattice_springs(int nx, int ny, int nz);
 int titan_gb300_lattice(const double center[3], const double dims[3], int nx, int ny, int nz,
                         double *pos, int32_t *left, int32_t *right, double *rest);

@@ -223,3 +223,19 @@ class OracleSim:
 
 def host_threads() -> int:
     return int(os.environ.get("OMP_NUM_THREADS") or os.cpu_count() or 1)
+
+
+def stl_inside(tri, pts, num_rays=5, seed=1, nthreads=0):
+    """Oracle of STL point-in-mesh classification (see titan_oracle.h)."""
+    L = lib()
+    L.to_stl_inside.argtypes = [_D, ctypes.c_int64, _D, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64,
+                                _U8, ctypes.c_int]
+    tri = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+    out = np.zeros(pts.shape[0], np.uint8)
+    rc = L.to_stl_inside(tri.ctypes.data_as(_D), tri.shape[0], pts.ctypes.data_as(_D), pts.shape[0], num_rays,
+                         seed, out.ctypes.data_as(_U8), nthreads or host_threads())
+    if rc:
+        raise ValueError("to_stl_inside failed")
+    return out.astype(bool)
+

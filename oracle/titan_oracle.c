@@ -542,3 +542,70 @@ void to_momentum(const to_scene *s, double lin[3], double ang[3]) {
         ang[2] = ang[2] + (p[0] * x[1] - p[1] * x[0]);
     }
 }
+
+/* ---- STL point-in-mesh (include/Titan/stlparser.h:213-276) --------------- */
+
+static uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+}
+
+static double ray_component(uint64_t seed, int64_t point, int ray, int c) {
+    const uint64_t k = splitmix64(seed ^ splitmix64((uint64_t)point * 3ULL * 64ULL + (uint64_t)ray * 3ULL + (uint64_t)c));
+    const double u = (double)(k >> 11) * (1.0 / 9007199254740992.0);
+    return -1000.0 + u * 2000.0;
+}
+
+static double sdot(const double *a, const double *b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+static void scross(const double *a, const double *b, double *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = b[0] * a[2] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static int ray_hits(const double *p, const double *ray, const double *t) {
+    const double eps = 0.000001;
+    const double e1[3] = {t[3] - t[0], t[4] - t[1], t[5] - t[2]};
+    const double e2[3] = {t[6] - t[0], t[7] - t[1], t[8] - t[2]};
+    double h[3], q[3];
+    scross(ray, e2, h);
+    const double a = sdot(e1, h);
+    if (a > -eps && a < eps) return 0;
+    const double f = 1 / a;
+    const double s[3] = {p[0] - t[0], p[1] - t[1], p[2] - t[2]};
+    const double u = f * sdot(s, h);
+    if (u < 0 || u > 1.0) return 0;
+    scross(s, e1, q);
+    const double v = f * sdot(ray, q);
+    if (v < 0 || u + v > 1.0) return 0;
+    return f * sdot(e2, q) > eps;
+}
+
+int to_stl_inside(const double *tri, int64_t ntri, const double *pts, int64_t npts, int num_rays, uint64_t seed,
+                  uint8_t *inside, int nthreads) {
+    if (num_rays < 1 || num_rays > 64) return -1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < npts; i++) {
+        int odd = 0;
+        for (int r = 0; r < num_rays; r++) {
+            double d[3];
+            for (int c = 0; c < 3; c++) d[c] = ray_component(seed, i, r, c);
+            const double n = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+            const double ray[3] = {d[0] / n, d[1] / n, d[2] / n};
+            int par = 0;
+            for (int64_t t = 0; t < ntri; t++) par ^= ray_hits(pts + 3 * i, ray, tri + 9 * t);
+            odd += par;
+        }
+        inside[i] = (double)odd / (double)num_rays > 0.5 ? 1 : 0;
+    }
+    return 0;
+}
+

@@ -91,6 +91,15 @@ enum { TO_EULER = 0, TO_VERLET = 1, TO_RK2 = 2 };
  * after each (src/sim.cu:1572-1583).  Returns 0 on success. */
 int to_step(to_scene *s, int64_t nsteps, int order, int nthreads);
 
+/* Point-in-mesh classification of STL import (stl::stlFile::inside,
+ * include/Titan/stlparser.h:213-276): inside when more than half of num_rays
+ * rays cross the mesh an odd number of times; ray r of point i is three
+ * uniform values in [-1000, 1000) from SplitMix64(seed, i, r) divided by its
+ * norm (the reference draws them with rand()).  tri: 9 doubles per triangle;
+ * pts: 3 per point; inside: 1 byte per point.  num_rays <= 64. */
+int to_stl_inside(const double *tri, int64_t ntri, const double *pts, int64_t npts, int num_rays, uint64_t seed,
+                  uint8_t *inside, int nthreads);
+
 /* Spring force on the RIGHT endpoint (src/sim.cu:1054-1065); the left one gets
  * its negation. */
 void to_spring_force(const double *pl, const double *pr, const double *vl, const double *vr,

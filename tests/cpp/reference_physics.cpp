@@ -6,6 +6,7 @@
 #include <Titan/sim.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <iostream>
@@ -249,6 +250,71 @@ static void topology_edit_test() {
     sim.stop();
 }
 
+// importFromSTL (src/sim.cu:1855-1921): a binary STL of an L-shaped solid
+// (two closed boxes, [0,2]x[0,1]x[0,1] and [0,1]x[1,2]x[0,1]) written here;
+// the bounding box [0,2]x[0,2]x[0,1] gets a 10^3 lattice, and the masses in
+// the missing quadrant are dropped with their springs.
+static void stl_import_test() {
+    const char *path = "/tmp/titan_gb300_stl_import_test.stl";
+    {
+        FILE *f = std::fopen(path, "wb");
+        EXPECT_TRUE(f != nullptr);
+        if (!f) return;
+        char header[80] = {0};
+        std::fwrite(header, 1, 80, f);
+        const uint32_t n = 24;
+        std::fwrite(&n, 4, 1, f);
+        const float boxes[2][2][3] = {{{0, 0, 0}, {2, 1, 1}}, {{0, 1, 0}, {1, 2, 1}}};
+        const int q[6][4] = {{0, 2, 3, 1}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 6, 7, 3}, {0, 4, 6, 2}, {1, 3, 7, 5}};
+        for (const auto &b : boxes) {
+            float c[8][3];
+            for (int i = 0; i < 8; i++)
+                for (int d = 0; d < 3; d++) c[i][d] = ((i >> d) & 1) ? b[1][d] : b[0][d];
+            for (const auto &quad : q)
+                for (int h = 0; h < 2; h++) {
+                    const int v[3] = {quad[0], quad[h + 1], quad[h + 2]};
+                    float rec[12] = {0, 0, 0};
+                    for (int k = 0; k < 3; k++)
+                        for (int d = 0; d < 3; d++) rec[3 + 3 * k + d] = c[v[k]][d];
+                    const uint16_t attr = 0;
+                    std::fwrite(rec, 4, 12, f);
+                    std::fwrite(&attr, 2, 1, f);
+                }
+        }
+        std::fclose(f);
+    }
+    titan::Simulation sim;
+    // density 2.1: num_pts = (int) cbrt(2.1 * (10 / 2)^3 * 2 * 2 * 1) = 10
+    titan::Container *c = sim.importFromSTL(path, 2.1, 5);
+    std::remove(path);
+    // lattice point (px, py, pz) maps to (1 + 0.2 px, 1 + 0.2 py, 0.2 (pz - 5) + 0.5)
+    int kept_expected = 0;
+    for (int i = 0; i < 10; i++)
+        for (int j = 0; j < 10; j++) {
+            const double x = 1 + 0.2 * (-4.9995 + i * 9.999 / 9), y = 1 + 0.2 * (-4.9995 + j * 9.999 / 9);
+            if (y < 1 || x < 1) kept_expected += 10;
+        }
+    EXPECT_TRUE((int)c->masses.size() == kept_expected);
+    for (titan::Mass *m : c->masses) {
+        const double x = 1.0 + 0.2 * m->pos[0], y = 1.0 + 0.2 * m->pos[1];
+        EXPECT_TRUE(y < 1 || x < 1);
+    }
+    for (titan::Spring *sp : c->springs) {
+        bool l = false, r = false;
+        for (titan::Mass *m : c->masses) {
+            l = l || m == sp->_left;
+            r = r || m == sp->_right;
+        }
+        EXPECT_TRUE(l && r);
+    }
+    EXPECT_TRUE(sim.masses.size() == c->masses.size() && sim.springs.size() == c->springs.size());
+    sim.start();
+    sim.pause(0.01);
+    sim.getAll();
+    EXPECT_TRUE(std::isfinite(c->masses[0]->pos[2]) && c->masses[0]->pos[2] < 10.0);
+    sim.stop();
+}
+
 int main(int argc, char **argv) {
     std::map<std::string, void (*)()> tests = {
         {"simple_test", simple_test},         {"energy_test", energy_test},
@@ -257,6 +323,7 @@ int main(int argc, char **argv) {
         {"breakpoint_and_step_test", breakpoint_and_step_test},
         {"beam_fixed_face_test", beam_fixed_face_test},
         {"topology_edit_test", topology_edit_test},
+        {"stl_import_test", stl_import_test},
     };
     if (argc < 2 || !tests.count(argv[1])) {
         for (auto &kv : tests) std::printf("%s\n", kv.first.c_str());

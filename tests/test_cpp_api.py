@@ -15,7 +15,7 @@ OUT = ROOT / "tests" / "cpp" / "_build" / "reference_physics"
 PKG = ROOT / "titan_gb300"
 
 TESTS = ["simple_test", "energy_test", "external_test", "external_acc_test", "multiagent_test", "rotate_test",
-         "breakpoint_and_step_test", "beam_fixed_face_test", "topology_edit_test"]
+         "breakpoint_and_step_test", "beam_fixed_face_test", "topology_edit_test", "stl_import_test"]
 
 
 def compile_tests():

@@ -90,6 +90,8 @@ _SIGS = {
     "titan_gb300_lattice_springs": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "titan_gb300_lattice": (ctypes.c_int, [_D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _I32, _I32, _D]),
     "titan_gb300_version": (ctypes.c_char_p, []),
+    "titan_gb300_stl_inside": (ctypes.c_int, [ctypes.c_int, _D, ctypes.c_int64, _D, ctypes.c_int64, ctypes.c_int,
+                                              ctypes.c_uint64, _U8]),
 }
 
 
@@ -433,3 +435,18 @@ class Sim:
         keys = ["masses", "springs", "tiles", "entries", "halo", "inc_words", "heavy", "smem_bytes", "threads",
                 "algorithmic_bytes_per_step", "implementation_bytes_per_step", "actuated_entries"]
         return {k: int(v) for k, v in zip(keys, out)}
+
+
+def stl_inside(tri, pts, num_rays: int = 5, seed: int = 1, device: int = 0) -> np.ndarray:
+    """Point-in-mesh test of STL import on the GPU (titan_gb300_stl_inside):
+    tri (T, 9) or (T, 3, 3) triangle vertices, pts (N, 3); True where more than
+    half of num_rays random rays cross the mesh an odd number of times."""
+    tri = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 3)
+    out = np.zeros(pts.shape[0], np.uint8)
+    rc = lib().titan_gb300_stl_inside(device, _ptr(tri, ctypes.c_double), tri.shape[0], _ptr(pts, ctypes.c_double),
+                                      pts.shape[0], num_rays, seed, _ptr(out, ctypes.c_uint8))
+    if rc:
+        raise TitanError(rc, "stl_inside")
+    return out.astype(bool)
+

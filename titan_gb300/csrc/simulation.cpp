@@ -7,7 +7,11 @@
 // reference's GPU thread (src/sim.cu:1389) becomes a request loop that runs
 // CUDA-graph chunks between breakpoints and yields to get/set between chunks.
 #include <algorithm>
+#include <cfloat>
 #include <chrono>
+#include <cmath>
+#include <cstring>
+#include <fstream>
 #include <cstdlib>
 #include <iostream>
 #include <map>
@@ -267,8 +271,94 @@ Beam *Simulation::createBeam(const Vec &center, const Vec &dims, int nx, int ny,
     return b;
 }
 
-Container *Simulation::importFromSTL(const std::string &, double, int) {
-    throw std::runtime_error("importFromSTL: STL voxelisation is not part of the titan_gb300 engine");
+// Seed of the point-in-mesh rays (the reference draws them with rand()).
+constexpr uint64_t kStlSeed = 0x7469746e53544cULL;
+
+// Simulation::importFromSTL, src/sim.cu:1855-1921: a num_pts^3 lattice over
+// the mesh's bounding box, scaled so that its longest side is 10, keeps the
+// masses whose point the mesh contains (titan_gb300_stl_inside, on the GPU)
+// and the springs between kept masses.  Binary STL as the reference parses it
+// (include/Titan/stlparser.h:300-333): an 80-byte header, a uint32 count,
+// then per triangle 12 little-endian floats (normal, v1, v2, v3) and a
+// 2-byte attribute.
+Container *Simulation::importFromSTL(const std::string &path, double density, int num_rays) {
+    if (ENDED) throw std::runtime_error("The simulation has ended. Cannot import new STL objects");
+    std::ifstream f(path.c_str(), std::ios::in | std::ios::binary);
+    if (!f) throw std::runtime_error("importFromSTL: cannot read " + path);
+    char header[80];
+    unsigned char cnt[4];
+    f.read(header, 80);
+    f.read(reinterpret_cast<char *>(cnt), 4);
+    if (!f) throw std::runtime_error("importFromSTL: " + path + " is not a binary STL file");
+    const uint32_t ntri = (uint32_t)cnt[0] | ((uint32_t)cnt[1] << 8) | ((uint32_t)cnt[2] << 16) | ((uint32_t)cnt[3] << 24);
+    std::vector<double> tri(9 * (size_t)ntri);
+    for (uint32_t t = 0; t < ntri; t++) {
+        unsigned char rec[50];
+        f.read(reinterpret_cast<char *>(rec), 50);
+        if (!f) throw std::runtime_error("importFromSTL: " + path + " is truncated");
+        for (int k = 0; k < 9; k++) {
+            const unsigned char *b = rec + 12 + 4 * k;
+            const uint32_t bits = (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+            float v;
+            std::memcpy(&v, &bits, 4);
+            tri[9 * (size_t)t + k] = v;
+        }
+    }
+    // bounding box as stlFile::getBoundingBox computes it (stlparser.h:193-210),
+    // including its starting values {DBL_MIN, 0, 0} for both corners
+    double mn[3] = {DBL_MIN, 0.0, 0.0}, mx[3] = {DBL_MIN, 0.0, 0.0};
+    for (size_t q = 0; q < tri.size(); q += 3)
+        for (int i = 0; i < 3; i++) {
+            mn[i] = std::fmin(tri[q + i], mn[i]);
+            mx[i] = std::fmax(tri[q + i], mx[i]);
+        }
+    const double center[3] = {(mx[0] - mn[0]) / 2 + mn[0], (mx[1] - mn[1]) / 2 + mn[1], (mx[2] - mn[2]) / 2 + mn[2]};
+    const double xdim = mx[0] - mn[0], ydim = mx[1] - mn[1], zdim = mx[2] - mn[2];
+    const double dimmax = std::max(std::max(xdim, ydim), zdim);
+    const double dimx = 10 * xdim / dimmax, dimy = 10 * ydim / dimmax, dimz = 10 * zdim / dimmax;
+    const int num_pts = (int)std::cbrt(density * std::pow(10 / dimmax, 3) * xdim * ydim * zdim);
+    if (!(num_pts >= 2)) throw std::runtime_error("importFromSTL: density gives fewer than 2 lattice points per side");
+    Lattice *l1 = new Lattice(Vec(0, 0, dimz), Vec(dimx - 0.001, dimy - 0.001, dimz - 0.001), num_pts, num_pts,
+                              num_pts);
+    const size_t n = l1->masses.size();
+    std::vector<double> pts(3 * n);
+    for (size_t i = 0; i < n; i++) {
+        const Mass *m = l1->masses[i];
+        pts[3 * i] = center[0] + (xdim / dimx) * m->pos[0];
+        pts[3 * i + 1] = center[1] + (ydim / dimy) * m->pos[1];
+        pts[3 * i + 2] = (zdim / dimz) * (m->pos[2] - dimz) + center[2];
+    }
+    std::vector<uint8_t> in(n, 0);
+    const int rc = titan_gb300_stl_inside(0, tri.data(), (int64_t)ntri, pts.data(), (int64_t)n, num_rays, kStlSeed,
+                                          in.data());
+    if (rc != TITAN_GB300_OK) {
+        delete l1;
+        throw std::runtime_error("importFromSTL: the point-in-mesh test failed (status " + std::to_string(rc) + ")");
+    }
+    std::unordered_map<const Mass *, bool> keep;
+    for (size_t i = 0; i < n; i++) keep[l1->masses[i]] = in[i] != 0;
+    std::vector<Spring *> springs_kept;
+    for (Spring *sp : l1->springs) {
+        if (keep[sp->_left] && keep[sp->_right])
+            springs_kept.push_back(sp);
+        else
+            delete sp;
+    }
+    std::vector<Mass *> masses_kept;
+    for (Mass *m : l1->masses) {
+        if (keep[m])
+            masses_kept.push_back(m);
+        else
+            delete m;
+    }
+    l1->springs = springs_kept;
+    l1->masses = masses_kept;
+    masses.reserve(masses.size() + l1->masses.size());
+    springs.reserve(springs.size() + l1->springs.size());
+    for (Mass *m : l1->masses) createMass(m);
+    for (Spring *sp : l1->springs) createSpring(sp);
+    containers.push_back(l1);
+    return l1;
 }
 
 void Simulation::createPlane(const Vec &abc, double d) { createPlane(abc, d, 0.0, 0.0); }
