@@ -469,9 +469,10 @@ int build_device(titan_gb300_sim *s) {
         ti.inc_off = (int32_t)i0;
         ti.inc_words = (int32_t)(i1 - i0);
         ti.pad0 = ti.pad1 = ti.pad2 = 0;
+        // ne + 1 force slots: the last holds the zero force padding codes name
         s->smem = std::max(s->smem, s->kernel_req == 3
-                                        ? tg::tile_async_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy)
-                                        : tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne, ti.nheavy));
+                                        ? tg::tile_async_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy)
+                                        : tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy));
         max_ne = std::max<int64_t>(max_ne, ti.ne);
         max_nact = std::max<int64_t>(max_nact, ti.nact);
         max_incw = std::max<int64_t>(max_incw, ti.inc_words);
@@ -551,7 +552,7 @@ int build_device(titan_gb300_sim *s) {
         }
         tg::WsLayout &W = a.ws;
         W.slots = (int32_t)al(mS * rec, 16);
-        W.act = (int32_t)al(W.slots + mE * ent, 16);
+        W.act = (int32_t)al(W.slots + (mE + 1) * ent, 16);  // + the zero slot padding codes name
         W.inc = (int32_t)al(W.act + mA * ent, 16);
         W.stage = (int32_t)al(W.inc + mI * 2, 128);
         W.idx_words = (int32_t)al(mNh, 4);

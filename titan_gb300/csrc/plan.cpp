@@ -166,7 +166,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 if (fits) {
                     int64_t heavy = 0;
                     for (int64_t m = lo; m < hi; m++) heavy += (ip[m + 1] - ip[m]) > in.heavy_threshold;
-                    fits = (nm + (int64_t)halo.size()) * in.slot_bytes + ne * in.entry_bytes +
+                    fits = (nm + (int64_t)halo.size()) * in.slot_bytes + (ne + 1) * in.entry_bytes +
                                heavy * in.heavy_bytes <= in.smem_budget;
                 }
             }
@@ -215,7 +215,9 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     return "incidence table exceeds 2^32 words";
                 uint32_t off = (uint32_t)P.inc.size();
                 P.warp_inc_off.push_back(off);
-                P.inc.resize(P.inc.size() + (size_t)(width * 32), 0);
+                // padding codes name slot ne, one past the tile's entries: a
+                // kernel that keeps a zero force there can sum whole words
+                P.inc.resize(P.inc.size() + (size_t)(width * 32), (uint16_t)ne);
                 for (int64_t m = m0; m < m1; m++) {
                     int64_t d = ip[m + 1] - ip[m];
                     int64_t lane = m - m0;

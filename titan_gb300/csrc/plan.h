@@ -64,7 +64,7 @@ struct Plan {
     std::vector<int64_t> tile_warp_off;      // ntiles+1 (global warp index)
     std::vector<uint32_t> warp_inc_off;      // per warp, into inc (u16 words)
     std::vector<uint8_t> deg;                // per new mass; 255 = heavy
-    std::vector<uint16_t> inc;               // entry | 0x8000 when the mass is the left end
+    std::vector<uint16_t> inc;               // entry | 0x8000 when the mass is the left end; padding: ne
     std::vector<int64_t> tile_heavy_off;     // ntiles+1 (global heavy index)
     std::vector<uint16_t> heavy_local;       // tile-local index of each heavy mass
     std::vector<uint32_t> heavy_inc_off;     // nheavy+1, into heavy_inc

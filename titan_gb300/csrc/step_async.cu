@@ -47,9 +47,9 @@ __global__ void __launch_bounds__(512) k_step_async(StepArgs a, int parity, int 
     const int S = ti.nm + ti.nh, E = ti.ne;
     uint8_t *st = smem;
     uint8_t *slots = smem + al16((int64_t)S * kRec);
-    R *sH = reinterpret_cast<R *>(slots + (int64_t)E * kSlot);
+    R *sH = reinterpret_cast<R *>(slots + (int64_t)(E + 1) * kSlot);  // after the zero slot
     uint64_t *bar = reinterpret_cast<uint64_t *>(
-        smem + al16(al16((int64_t)S * kRec) + (int64_t)E * kSlot + 3 * (int64_t)ti.nheavy * (int64_t)sizeof(R)));
+        smem + al16(al16((int64_t)S * kRec) + (int64_t)(E + 1) * kSlot + 3 * (int64_t)ti.nheavy * (int64_t)sizeof(R)));
     const uint8_t *in = reinterpret_cast<const uint8_t *>(parity ? a.state1 : a.state0);
     void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
@@ -129,6 +129,12 @@ __global__ void __launch_bounds__(512) k_step_async(StepArgs a, int parity, int 
             entry_force<PREC>(rr, actuated, qq, st, t, slots + (int64_t)e * kSlot);
         }
     }
+    // the zero force that padding incidence codes name (slot E)
+    if (threadIdx.x == 0) {
+        reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (kSlot == 32)
+            reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     __syncthreads();
 
     // ---- C0: heavy masses --------------------------------------------------
@@ -163,7 +169,7 @@ __global__ void __launch_bounds__(512) k_step_async(StepArgs a, int parity, int 
                     if (w0 + k < nw) cw[k] = __ldcs(ip + 32 * (w0 + k));
 #pragma unroll
                 for (int k = 0; k < kBatchC; k++)
-                    if (w0 + k < nw) gather_word<PREC>(slots, cw[k], w0 + k, d, F0, F1, F2);
+                    if (w0 + k < nw) gather_word_padded<PREC>(slots, cw[k], F0, F1, F2);
             }
         }
         St<PREC> s = load_state_smem<PREC>(st, i);

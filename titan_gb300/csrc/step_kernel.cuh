@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
     const int S = ti.nm + ti.nh, E = ti.ne;
     uint8_t *st = smem;                                   // S state records
     uint8_t *slots = smem + align16((int64_t)S * kRec);   // E force slots
-    R *sH = reinterpret_cast<R *>(slots + (int64_t)E * kSlot);  // 3 * nheavy
+    R *sH = reinterpret_cast<R *>(slots + (int64_t)(E + 1) * kSlot);  // 3 * nheavy, after the zero slot
     const uint8_t *in = reinterpret_cast<const uint8_t *>(parity ? a.state1 : a.state0);
     void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
@@ -142,6 +142,12 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
             }
         }
     }
+    // the zero force that padding incidence codes name (slot E)
+    if (threadIdx.x == 0) {
+        reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (kSlot == 32)
+            reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     __syncthreads();
 
     // ---- C0: heavy masses --------------------------------------------------
@@ -173,7 +179,7 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
             if (own) {
 #pragma unroll
                 for (int w = 0; w < kPrefetchW; w++)
-                    if ((uint32_t)w < nw) gather_word<PREC>(slots, cw_own[w], w, d, F0, F1, F2);
+                    if ((uint32_t)w < nw) gather_word_padded<PREC>(slots, cw_own[w], F0, F1, F2);
                 w0 = kPrefetchW;
             }
             for (; w0 < nw; w0 += kBatchC) {
@@ -183,7 +189,7 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
                     if (w0 + k < nw) cw[k] = __ldcs(ip + 32 * (w0 + k));
 #pragma unroll
                 for (int k = 0; k < kBatchC; k++)
-                    if (w0 + k < nw) gather_word<PREC>(slots, cw[k], w0 + k, d, F0, F1, F2);
+                    if (w0 + k < nw) gather_word_padded<PREC>(slots, cw[k], F0, F1, F2);
             }
         }
         St<PREC> s = load_state_smem<PREC>(st, i);

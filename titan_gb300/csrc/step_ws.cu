@@ -68,10 +68,15 @@ __device__ __forceinline__ bool group_any(int id, int nthreads, bool v) {
 }
 
 // Bounded wait; gives up early when another warp raised the abort word.
-__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word) {
+// sleep_ns > 0 backs off between polls (the producer, which runs ahead,
+// waits this way so that its polling does not take issue slots from the
+// consumers on its scheduler).
+__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word,
+                                        unsigned sleep_ns = 0) {
     for (uint32_t it = 0; it < kWaitLimit; it++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255u) == 255u && *abort_word) return false;
+        if (sleep_ns) __nanosleep(sleep_ns);
     }
     return false;
 }
@@ -147,7 +152,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
             const bool has_next = t + G < ntiles;
             TileInfo tn = {};
             if (has_next) tn = a.tiles[t + G];
-            bool ok = ws_wait(&empty[s], ph ^ 1u, abort_word);
+            bool ok = ws_wait(&empty[s], ph ^ 1u, abort_word, 200);
             if (ok) {
                 ok = ws_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
                 if (ok && lane == 0) *idx_waited = k + 1;
@@ -240,6 +245,12 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                     if (e < E) entry_force<PREC>(r[j], e < ti.nact, q[j], st, tm, slots + (int64_t)e * kSlot);
                 }
             }
+            // the zero force that padding codes name (slot E)
+            if (gt == 0) {
+                reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (kSlot == 32)
+                    reinterpret_cast<float4 *>(slots + (int64_t)E * kSlot)[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
             group_sync(bar_id, gn);
 
             // ---- C0: heavy masses ----
@@ -268,7 +279,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                         (own ? woff_own : __ldg(a.warp_inc_off + ti.warp_off + (i >> 5))) - (uint32_t)ti.inc_off;
                     const uint2 *ip = reinterpret_cast<const uint2 *>(incs + woff) + (i & 31);
                     const uint32_t nw = (d + 3) >> 2;
-                    for (uint32_t w = 0; w < nw; w++) gather_word<PREC>(slots, ip[32 * w], w, d, F0, F1, F2);
+                    for (uint32_t w = 0; w < nw; w++) gather_word_padded<PREC>(slots, ip[32 * w], F0, F1, F2);
                 }
                 St<PREC> sv = load_state_smem<PREC>(st, i);
                 integrate<PREC, INTEG>(a, ti, g, fl, m, F0, F1, F2, sv, out, g, write_acc, np, prm);

@@ -213,6 +213,34 @@ __device__ __forceinline__ void gather_word(const uint8_t *slots, uint2 cw, uint
     }
 }
 
+// The same for a whole word: codes past the mass's degree are padding that
+// names a slot holding a zero force (+0 adds nothing: the running sum is a
+// finite force or +0 after the first code).
+template <int PREC>
+__device__ __forceinline__ void gather_word_padded(const uint8_t *slots, uint2 cw, typename Real<PREC>::T &F0,
+                                                   typename Real<PREC>::T &F1, typename Real<PREC>::T &F2) {
+#pragma unroll
+    for (int h = 0; h < 4; h++) {
+        const uint32_t word = h < 2 ? cw.x : cw.y;
+        const uint32_t code = (h & 1) ? (word >> 16) : (word & 0xffffu);
+        const int idx = code & 0x7fff;
+        if constexpr (PREC == P_FP64) {
+            const double sg = (code & 0x8000) ? -1.0 : 1.0;
+            const double2 *f = reinterpret_cast<const double2 *>(slots + (int64_t)idx * 32);
+            const double2 f01 = f[0], f2v = f[1];
+            F0 = fma(sg, f01.x, F0);
+            F1 = fma(sg, f01.y, F1);
+            F2 = fma(sg, f2v.x, F2);
+        } else {
+            const float sg = (code & 0x8000) ? -1.0f : 1.0f;
+            const float4 f = reinterpret_cast<const float4 *>(slots)[idx];
+            F0 = fmaf(sg, f.x, F0);
+            F1 = fmaf(sg, f.y, F1);
+            F2 = fmaf(sg, f.z, F2);
+        }
+    }
+}
+
 // Warp-cooperative, fixed-order sum over a heavy mass's incidence list
 // (lane l takes codes l, l+32, ...; then an xor butterfly).
 // warp / nw: this warp's index among the nw warps sharing the work.
