@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=400)
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-max-masses", type=int, default=200000)
+    p.add_argument("--serve-small-masses", type=int, default=50000,
+                   help="requests below this many masses run the per-tile kernel (0: all automatic)")
     p.add_argument("--ref-gpu-steps", type=int, default=50,
                    help="steps of the reference's own CUDA kernels timed beside ours (0: skip)")
     return p.parse_args()
@@ -504,7 +506,7 @@ def run_serving(a, local):
     reqs = wl.config5(a.serve_requests, a.serve_rate, mass_range=(27, a.serve_max_masses))
     # scenes built before the clock starts (request payloads arrive ready)
     scenes = {r["id"]: wl.rollout_request(r["side"], r["seed"]) for r in reqs}
-    srv = serving.RolloutServer(prec, device=local)
+    srv = serving.RolloutServer(prec, device=local, small_masses=a.serve_small_masses)
     # warm-up: one request per design, so that the served run measures
     # steady state (plans, engines and graphs exist)
     warm = {}

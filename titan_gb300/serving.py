@@ -30,8 +30,14 @@ from . import workloads as wl
 
 
 class RolloutServer:
-    def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_active=256, pool_per_design=64):
+    def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_active=256, pool_per_design=64,
+                 small_masses=50000):
+        """small_masses: scenes below this size run the per-tile kernel with
+        128-mass tiles (a few CTAs per SM, so that many small rollouts share
+        the SMs); larger ones the automatic kernel (one persistent CTA per
+        SM).  0 disables the split."""
         self.precision = precision
+        self.small_masses = small_masses
         self.device = device
         self.budget = float(hbm_budget_bytes)
         self.max_active = max_active
@@ -59,15 +65,17 @@ class RolloutServer:
                                 omega=sc["omega"], amp=sc["amp"], phase=sc["phase"])
             e.set_time(0.0)
             return e
+        small = sc["pos"].shape[0] < self.small_masses
+        kernel, tile = (1, 128) if small else (0, 0)
         if side not in self.templates:
             t = Sim(self.precision, self.device)
-            wl.load(t, sc, start=False)
-            t.plan_host()
+            wl.load(t, sc, start=False, kernel=kernel)
+            t.plan_host(tile)
             self.templates[side] = t
         e = Sim(self.precision, self.device)
-        wl.load(e, sc, start=False)
+        wl.load(e, sc, start=False, kernel=kernel)
         e.adopt_plan(self.templates[side])
-        e.start()
+        e.start(tile)
         self.engines_built += 1
         if side not in self.bytes_of:
             self.bytes_of[side] = float(e.device_bytes())
