@@ -193,18 +193,30 @@ int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
  * persistent launch per step() call runs all nsteps steps of every bin with
  * the state held in shared memory; the remaining bodies take the per-step
  * kernels.  Results are bit-identical to the per-step kernels.
- *   mode 0: off (default: on GB300 the per-step kernels measured faster
- *   for batches whose spring records exceed shared memory); 1 on.  bin_masses: bin capacity, rounded up to a multiple of 32 (0:
- *   max(1024, largest fitting body)); bodies above it are not resident.
- *   threads_per_cta
- *   0: derived from the bin size; else a multiple of 32 in [64, 512].
+ *   mode -1 (default): automatic -- resident tiles (mode 2) when the
+ *   kernel form is automatic (set_kernel 0), the integrator is symplectic
+ *   Euler and every tile of the scene is halo-free (measured on GB300: 2.5x
+ *   faster than the per-step kernels on one 125-mass body, 2x on thousands
+ *   of small bodies, equal in FP64), else off; 0 off; 1 bins of
+ *   whole bodies, one thread per mass (bin_masses: bin capacity, rounded
+ *   up to a multiple of 32; 0: the largest fitting body when at most 152
+ *   bodies fit, else max(1024, largest fitting body); bodies above it are
+ *   not resident); 2 resident tiles: every tile with no halo (all springs
+ *   of its masses inside it) is stepped by one CTA for all steps of a call
+ *   with the per-step kernels' two phases in shared memory, its slab,
+ *   actuation and incidence records staged there too when they fit and
+ *   every such tile still gets a CTA at once (bin_masses unused; the tile
+ *   size is start()'s).  threads_per_cta 0: derived from the bin or tile
+ *   size; else a multiple of 32 in [64, 512].  Symplectic Euler only: the
+ *   other integrators run every tile on the per-step kernels.
  * Set before start(). */
 int titan_gb300_set_resident(titan_gb300_sim *sim, int mode, int bin_masses, int threads_per_cta);
 
-/* After start(): out[0] 1 if resident bins are in use, out[1] bins,
- * out[2] resident bodies, out[3] resident masses, out[4] bin capacity
- * (masses), out[5] threads per CTA, out[6] CTAs per launch, out[7] dynamic
- * shared memory per CTA (bytes). */
+/* After start(): out[0] the resident form in use (0 none, 1 bins, 2
+ * tiles), out[1] bins or resident tiles, out[2] resident bodies, out[3]
+ * resident masses, out[4] bin capacity or largest resident tile (masses),
+ * out[5] threads per CTA, out[6] CTAs per launch, out[7] dynamic shared
+ * memory per CTA (bytes). */
 int titan_gb300_resident_info(const titan_gb300_sim *sim, int64_t out[8]);
 
 /* One iteration of the reference's execute() loop body (src/sim.cu:1569-1590)

@@ -303,10 +303,12 @@ def test_resident_plan_excludes_large_and_coupled_bodies():
 
 def test_set_resident_validates():
     s = tg.Sim(tg.FP32C)
-    for args in ((2, 0, 0), (-1, 0, 0), (1, -5, 0), (1, 0, 100), (1, 0, 1024)):
+    for args in ((3, 0, 0), (-2, 0, 0), (1, -5, 0), (1, 0, 100), (1, 0, 1024)):
         with pytest.raises(tg.TitanError, match="EINVAL"):
             s.set_resident(*args)
     s.set_resident(1, 512, 128)
+    s.set_resident(2)
+    s.set_resident(-1)
     s.set_resident(0)
     s.close()
 

@@ -1,4 +1,5 @@
-"""GPU parity of the body-resident batched launch (resident.cu).
+"""GPU parity of the resident launches: bins of whole bodies (resident.cu)
+and halo-free tiles (resident_tiles.cu).
 
 Bar: bit-identical to the per-step kernels in every precision, and in FP64
 (passive springs) to the oracle's ascending order -- max |diff| == 0 on
@@ -83,11 +84,11 @@ def test_resident_bins_beside_per_step_tiles_bitwise():
 
 
 @pytest.mark.parametrize("precision", [tg.FP64, tg.FP32, tg.FP32C])
-@pytest.mark.parametrize("shape", [(1, 0, 0), (1, 256, 64), (1, 512, 128)])
+@pytest.mark.parametrize("shape", [(1, 0, 0), (1, 256, 64), (1, 512, 128), (2, 0, 0), (2, 0, 64)])
 def test_resident_equals_per_step_kernels(precision, shape):
-    """Actuated bodies, a mid-run state upload: resident bins (several CTA
-    shapes, 1 to 4 masses per thread) and the per-step kernels agree bit
-    for bit."""
+    """Actuated bodies, a mid-run state upload: resident bins and resident
+    tiles (several CTA shapes, 1 to 4 masses per thread) and the per-step
+    kernels agree bit for bit."""
     sc = batch(nbodies=30, seed=14, side_range=(3, 8), passive=False)
     n = sc["pos"].shape[0]
     idx = np.arange(0, n, 7, dtype=np.int64)
@@ -115,3 +116,101 @@ def test_resident_only_scene_time_and_repeat():
     assert np.array_equal(a["pos"], o.pos) and np.array_equal(a["T"], o.T)
     s2, b = run(sc, [100])
     assert_same(a, b)
+
+
+def test_resident_tiles_fp64_bitwise_vs_oracle():
+    """Every body in one halo-free tile: the resident tiles carry the whole
+    scene, bit-identical to the oracle's ascending order in FP64."""
+    sc = batch(nbodies=40, seed=16, side_range=(3, 5))  # at most 125 masses: one FP64 tile (128) each
+    chunks = [1, 7, 64, 300, 128]
+    s, st = run(sc, chunks, resident=(2, 0, 0))
+    info = s.resident_info()
+    assert info["active"] == 2 and info["bodies"] == 40 and info["masses"] == sc["pos"].shape[0]
+    o = po.OracleSim(sc)
+    o.step(sum(chunks), po.ASCENDING, 1)
+    for k, v in (("pos", o.pos), ("vel", o.vel), ("acc", o.acc), ("T", o.T)):
+        assert np.array_equal(st[k], v), k
+    assert s.time == o.time
+
+
+def test_resident_tiles_beside_per_step_tiles_bitwise():
+    """Tiles of 64 masses: bodies larger than a tile (tiles with halos), and
+    two bodies joined by a spring, run on the per-step kernels in the same
+    step() calls as the halo-free tiles."""
+    sc = batch(nbodies=20, seed=17, side_range=(3, 8))
+    bp = sc["body_ptr"]
+    for key, val in (("left", bp[0]), ("right", bp[1]), ("k", 500.0), ("rest", 1.0), ("damping", 0.0), ("type", 0),
+                     ("omega", 0.0), ("amp", 0.2), ("phase", 0.0)):
+        sc[key] = np.concatenate([sc[key], [val]]).astype(sc[key].dtype)
+    chunks = [3, 250, 1, 146]
+    s, st = run(sc, chunks, resident=(2, 0, 0), tile=64)
+    info = s.resident_info()
+    sizes = np.diff(bp)
+    assert info["active"] == 2 and info["cap"] <= 64
+    assert info["bodies"] == int(np.sum(sizes[2:] <= 64))
+    assert 0 < s.kernel_info()["ctas"] < s.plan_info()["tiles"]
+    o = po.OracleSim(sc)
+    o.step(sum(chunks), po.ASCENDING, 1)
+    for k, v in (("pos", o.pos), ("vel", o.vel), ("acc", o.acc), ("T", o.T)):
+        assert np.array_equal(st[k], v), k
+
+
+@pytest.mark.parametrize("precision", [tg.FP64, tg.FP32, tg.FP32C])
+def test_resident_tiles_single_body_with_contact(precision):
+    """The small-robot scene (one actuated 125-mass lattice on a friction
+    plane): one resident tile with its records staged in shared memory,
+    bit-identical to the per-step kernels over calls of any length."""
+    sc = wl.actuate(wl.config1(contact=True), np.random.default_rng(7), 0.3, 0.1)
+    chunks = [1, 63, 200, 2000]
+    s1, a = run(sc, chunks, precision, resident=(2, 0, 0))
+    i1 = s1.resident_info()
+    assert i1["active"] == 2 and i1["bins"] == 1 and i1["masses"] == 125
+    s2, b = run(sc, chunks, precision, resident=(0, 0, 0))
+    assert_same(a, b)
+
+
+def test_resident_tiles_heavy_hub_bitwise():
+    """A hub mass of degree 300 (warp-cooperative heavy sum) in a resident
+    tile: bit-identical to the oracle's device order in FP64."""
+    from tests.test_oracle import hub_scene
+    sc = hub_scene(degree=300)
+    s, st = run(sc, [1, 99, 400], resident=(2, 0, 0), tile=512)
+    assert s.resident_info()["active"] == 2
+    o = po.OracleSim(sc, heavy_threshold=96)
+    o.step(500, po.DEVICE, 1)
+    for k, v in (("pos", o.pos), ("vel", o.vel), ("acc", o.acc)):
+        assert np.array_equal(st[k], v), k
+
+
+def test_automatic_resident_tiles_choice():
+    """By default resident tiles carry a scene whose tiles are all
+    halo-free (symplectic Euler, automatic kernel form), and nothing else."""
+    small = wl.config1(contact=True)
+    s = wl.make_sim(small, tg.FP32C)
+    assert s.resident_info()["active"] == 2 and s.plan_info()["tiles"] == 1
+    s.close()
+    s = wl.make_sim(small, tg.FP32C, kernel=1)  # an explicit kernel form: per-step kernels
+    assert s.resident_info()["active"] == 0
+    s.close()
+    s = wl.make_sim(wl.config2(n_side=20), tg.FP32C)  # tiles with halos
+    assert s.resident_info()["active"] == 0
+    s.close()
+    sc = dict(small, integrator=tg.VERLET)
+    s = wl.make_sim(sc, tg.FP64)
+    assert s.resident_info()["active"] == 0
+    s.close()
+
+
+def test_set_integrator_leaves_resident_tiles_bitwise():
+    """A switch to RK2 after some Euler steps rebuilds the scene on the
+    per-step kernels: same bits as a run that never had resident tiles."""
+    sc = wl.actuate(wl.config1(contact=True), np.random.default_rng(8), 0.3, 0.1)
+    out = []
+    for res in ((2, 0, 0), (0, 0, 0)):
+        s = wl.make_sim(sc, tg.FP64, resident=res)
+        s.step(300)
+        s.set_integrator(tg.RK2)
+        s.step(200)
+        assert s.resident_info()["active"] == 0
+        out.append(s.get_state(acc=True, T=True))
+    assert_same(*out)

@@ -295,8 +295,12 @@ class Sim:
                 "smem_bytes": int(out[3])}
 
     def set_resident(self, mode: int = 1, bin_masses: int = 0, threads: int = 0):
-        """Resident bins for batched bodies: mode 0 off (default), 1 on; bin
-        capacity in masses and CTA size (0: default)."""
+        """Resident launches (all steps of a call in one kernel): mode -1
+        automatic (the default: halo-free tiles when every tile is one and
+        the kernel form is automatic), 0 off, 1 bins of whole bodies (one
+        thread per mass), 2 halo-free tiles (the per-step kernels' two
+        phases in shared memory); bin capacity in masses (mode 1) and CTA
+        size (0: default)."""
         self._check(self._L.titan_gb300_set_resident(self._h, mode, bin_masses, threads), "set_resident")
 
     def resident_info(self) -> dict:

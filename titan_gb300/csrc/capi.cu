@@ -61,6 +61,9 @@ struct DevMem {
 struct titan_gb300_sim {
     int device = 0, prec = P_FP64;
     cudaStream_t stream = nullptr;
+    // resident tiles run on side_stream beside the per-step kernels
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
 
     // host scene (creation order)
@@ -130,13 +133,19 @@ struct titan_gb300_sim {
     int ctas = 0;         // persistent grid of the pipelined kernel
     int *d_err = nullptr;
     // body-resident batched launch
-    int res_mode = 0;     // 0 off, 1 on
+    int res_mode = -1;    // -1 automatic, 0 off, 1 bins of whole bodies, 2 halo-free tiles
     int res_bin_req = 0;  // bin capacity in masses (0: default)
     int res_threads_req = 0;
     tg::ResPlan rplan;
     tg::ResArgs rargs{};
     bool use_res = false;
     int res_threads = 0, res_ctas = 0;
+    // resident tiles (mode 2): halo-free tiles stepped in shared memory
+    bool use_rtiles = false;
+    tg::TileResArgs rtargs{};
+    std::vector<tg::TileInfo> rtiles;
+    int rt_threads = 0, rt_mpt = 0;
+    size_t rt_smem = 0;
     // plan taken from another handle with the same topology (adopt_plan);
     // used by the first start() only
     bool plan_adopted = false;
@@ -178,6 +187,12 @@ struct titan_gb300_sim {
         if (stream) cudaStreamSynchronize(stream);
         free_device();
         if (stream) cudaStreamDestroy(stream);
+        if (side_stream) {
+            cudaStreamSynchronize(side_stream);
+            cudaStreamDestroy(side_stream);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
     }
 };
 
@@ -410,13 +425,17 @@ int resident_cap(const titan_gb300_sim *s) {
     const int rec = tg::state_record_bytes(s->prec);
     int lim = (int)(((227 * 1024 - 1024) / (2 * rec)) & ~31);
     lim = std::min(lim, tg::kResMaxMpt * (s->res_threads_req > 0 ? s->res_threads_req : 512));
-    int64_t big = 0;
+    int64_t big = 0, fit = 0;
     for (int64_t b = 0; b < nb; b++) {
         const int64_t m = s->body_ptr.empty() ? s->n : s->body_ptr[b + 1] - s->body_ptr[b];
-        if (m <= lim) big = std::max(big, m);
+        if (m <= lim) big = std::max(big, m), fit++;
     }
     if (big == 0) return 0;
-    const int cap = s->res_bin_req > 0 ? s->res_bin_req : (int)std::max<int64_t>(1024, big);
+    // default: bins of at least 1024 masses pack small bodies; with no more
+    // bodies than one wave of single-body bins (152 SMs), one body per bin
+    // of its own size (more CTAs, less shared memory each)
+    const int64_t dflt = fit <= 152 ? big : std::max<int64_t>(1024, big);
+    const int cap = s->res_bin_req > 0 ? s->res_bin_req : (int)dflt;
     return std::min(lim, (cap + 31) & ~31);
 }
 
@@ -509,9 +528,72 @@ int build_device(titan_gb300_sim *s) {
             }
         }
     }
+    // resident tiles: halo-free tiles run all the steps of a launch in shared
+    // memory, their slab, actuation and incidence records staged there too
+    // when the largest tile's fit and every tile still gets a CTA at once
+    s->use_rtiles = false;
+    s->rtiles.clear();
+    s->rtargs = tg::TileResArgs{};
+    std::vector<uint8_t> rt_flag(P.ntiles, 0);
+    // automatic: resident tiles when the kernel form is automatic and every
+    // tile is halo-free and fits (measured on GB300: 2.5x faster than the
+    // per-step kernels on one 125-mass body, 2x on thousands of them; equal
+    // in FP64)
+    const bool rt_auto = s->res_mode == -1 && s->kernel_req == 0;
+    bool all_free = P.ntiles > 0;
+    for (int64_t t = 0; t < P.ntiles && all_free; t++) all_free = tiles[t].nh == 0;
+    if ((s->res_mode == 2 || (rt_auto && all_free)) && s->integrator == tg::INTEG_EULER) {
+        const size_t kMaxSmem = 227 * 1024;
+        const int tcap = s->res_threads_req > 0 ? s->res_threads_req : 512;
+        int64_t max_nm = 0, max_ne = 0;
+        for (int64_t t = 0; t < P.ntiles; t++) {
+            const tg::TileInfo &ti = tiles[t];
+            if (ti.nh != 0 || ti.nm > tg::kResMaxMpt * tcap || tg::tile_resident_smem_bytes(s->prec, ti, 0) > kMaxSmem)
+                continue;
+            rt_flag[t] = 1;
+            s->rtiles.push_back(ti);
+            max_nm = std::max<int64_t>(max_nm, ti.nm);
+            max_ne = std::max<int64_t>(max_ne, ti.ne);
+        }
+        if (s->res_mode == -1 && (int64_t)s->rtiles.size() < P.ntiles) {  // automatic: all tiles or none
+            s->rtiles.clear();
+            std::fill(rt_flag.begin(), rt_flag.end(), 0);
+        }
+        if (!s->rtiles.empty()) {
+            int sms = 0, dev = 0;
+            CK(cudaGetDevice(&dev), "device");
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
+            // threads: a thread per mass of the largest tile; with fewer tiles
+            // than SMs, up to a quarter of its slab entries (phase B) -- in
+            // [64, 512] (measured on GB300: one 125-mass tile steps fastest
+            // with 288 threads, thousands of them with 128)
+            const int64_t want_t = (int64_t)s->rtiles.size() < sms ? std::max<int64_t>(max_nm, max_ne / 4) : max_nm;
+            s->rt_threads = s->res_threads_req > 0
+                                ? s->res_threads_req
+                                : (int)std::max<int64_t>(64, std::min<int64_t>(512, (want_t + 31) & ~int64_t(31)));
+            s->rt_mpt = (int)((max_nm + s->rt_threads - 1) / s->rt_threads);
+            size_t sm_st = 0, sm_pl = 0;
+            for (const tg::TileInfo &ti : s->rtiles) {
+                sm_st = std::max(sm_st, tg::tile_resident_smem_bytes(s->prec, ti, 1));
+                sm_pl = std::max(sm_pl, tg::tile_resident_smem_bytes(s->prec, ti, 0));
+            }
+            int stage = 0;
+            if (sm_st <= kMaxSmem && tg::tile_resident_prepare(s->prec, s->rt_mpt, 1, sm_st) == cudaSuccess) {
+                const int ps = tg::tile_resident_ctas_per_sm(s->prec, s->rt_mpt, 1, s->rt_threads, sm_st);
+                stage = ps > 0 && (int64_t)s->rtiles.size() <= (int64_t)sms * ps;
+            }
+            s->rt_smem = stage ? sm_st : sm_pl;
+            CK(tg::tile_resident_prepare(s->prec, s->rt_mpt, stage, s->rt_smem), "set resident-tile shared memory");
+            if (tg::tile_resident_ctas_per_sm(s->prec, s->rt_mpt, stage, s->rt_threads, s->rt_smem) <= 0)
+                return s->fail(TITAN_GB300_ELIMIT, "resident tiles do not fit one SM");
+            s->use_rtiles = true;
+            s->rtargs.ntiles = (int32_t)s->rtiles.size();
+            s->rtargs.stage = stage;
+        }
+    }
     std::vector<tg::TileInfo> tiles_run;
     for (int64_t t = 0; t < P.ntiles; t++)
-        if (!s->use_res || !s->rplan.tile_resident[t]) tiles_run.push_back(tiles[t]);
+        if ((!s->use_res || !s->rplan.tile_resident[t]) && !rt_flag[t]) tiles_run.push_back(tiles[t]);
     // shared-memory layout of the pipelined kernel (two stages)
     {
         auto al = [](int64_t x) { return (int32_t)((x + 15) & ~int64_t(15)); };
@@ -621,6 +703,7 @@ int build_device(titan_gb300_sim *s) {
         dst = p_;                                             \
     } while (0)
     DEVCOPY(a.tiles, tiles_run, "upload tiles");
+    if (s->use_rtiles) DEVCOPY(s->rtargs.tiles, s->rtiles, "upload resident tiles");
     if (s->use_res) {
         tg::ResPlan &R = s->rplan;
         tg::ResArgs &r = s->rargs;
@@ -666,6 +749,12 @@ int build_device(titan_gb300_sim *s) {
     if (!(a.state1 = s->mem.get(s->comps() * np * rs, e))) return s->cuda_fail(e, "alloc state");
     if (!(a.acc = s->mem.get(3 * np * rs, e))) return s->cuda_fail(e, "alloc acc");
     if (!(a.tbuf = (double *)s->mem.get(2 * sizeof(double), e))) return s->cuda_fail(e, "alloc time");
+    if (s->use_rtiles) {
+        if (!(s->rtargs.t0 = (const double *)s->mem.get(sizeof(double), e))) return s->cuda_fail(e, "alloc time");
+        if (!s->side_stream) CK(cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking), "create stream");
+        if (!s->ev_fork) CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming), "create event");
+        if (!s->ev_join) CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming), "create event");
+    }
     if (!(s->dprm = (tg::DevParams *)s->mem.get(sizeof(tg::DevParams), e))) return s->cuda_fail(e, "alloc params");
     a.prm = s->dprm;
     if (!(s->d_err = (int *)s->mem.get(sizeof(int), e))) return s->cuda_fail(e, "alloc error flag");
@@ -862,7 +951,7 @@ int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
 
 int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int threads_per_cta) {
     if (!s) return TITAN_GB300_EINVAL;
-    if (mode < 0 || mode > 1) return s->fail(TITAN_GB300_EINVAL, "resident mode must be 0 or 1");
+    if (mode < -1 || mode > 2) return s->fail(TITAN_GB300_EINVAL, "resident mode must be -1, 0, 1 or 2");
     if (bin_masses < 0 || bin_masses > 32767) return s->fail(TITAN_GB300_EINVAL, "bin size must be in [0, 32767]");
     if (threads_per_cta != 0 && (threads_per_cta < 64 || threads_per_cta > 512 || threads_per_cta % 32))
         return s->fail(TITAN_GB300_EINVAL, "threads per CTA must be 0 or a multiple of 32 in [64, 512]");
@@ -876,6 +965,25 @@ int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int t
 int titan_gb300_resident_info(const titan_gb300_sim *s, int64_t out[8]) {
     if (!s || !out) return TITAN_GB300_EINVAL;
     std::memset(out, 0, 8 * sizeof(int64_t));
+    if (s->use_rtiles) {
+        out[0] = 2;
+        out[1] = (int64_t)s->rtiles.size();
+        std::vector<int32_t> bodies;
+        int64_t nm = 0, cap = 0;
+        for (const tg::TileInfo &ti : s->rtiles) {
+            bodies.push_back(ti.body);
+            nm += ti.nm;
+            cap = std::max<int64_t>(cap, ti.nm);
+        }
+        std::sort(bodies.begin(), bodies.end());
+        out[2] = (int64_t)(std::unique(bodies.begin(), bodies.end()) - bodies.begin());
+        out[3] = nm;
+        out[4] = cap;
+        out[5] = s->rt_threads;
+        out[6] = (int64_t)s->rtiles.size();
+        out[7] = (int64_t)s->rt_smem;
+        return TITAN_GB300_OK;
+    }
     if (!s->use_res) return TITAN_GB300_OK;
     out[0] = 1;
     out[1] = s->rplan.nbins;
@@ -1090,11 +1198,11 @@ int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) {
     }
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
     CK(cudaStreamSynchronize(s->stream), "set integrator");
-    const bool was_res = s->use_res;
+    const bool was_res = s->use_res || s->use_rtiles;
     s->integrator = kind;
     s->dt_log.push_back({s->steps, s->dt, s->passes()});
     s->drop_graphs();
-    if (was_res) {  // resident bins run Euler only: rebuild without them
+    if (was_res) {  // resident bins and tiles run Euler only: rebuild without them
         int rc = pull_state(s);
         if (rc) return rc;
         return build_device(s);
@@ -1183,6 +1291,27 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
         CK(tg::launch_resident(s->prec, s->args, s->rargs, s->res_ctas, s->res_threads, s->parity, nsteps, 1,
                                s->args.ntiles == 0, s->stream),
            "launch resident bins");
+    bool joined = true;
+    if (s->use_rtiles) {
+        // the first step's time, copied before per-step kernels advance the record
+        CK(cudaMemcpyAsync(const_cast<double *>(s->rtargs.t0), s->args.tbuf + s->parity, sizeof(double),
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "launch resident tiles");
+        if (s->args.ntiles == 0) {
+            CK(tg::launch_tile_resident(s->prec, s->args, s->rtargs, s->rt_mpt, s->rt_threads, s->rt_smem,
+                                        s->parity, nsteps, 1, s->stream),
+               "launch resident tiles");
+            CK(tg::launch_advance_time(s->args, s->parity, nsteps, s->stream), "advance time");
+        } else {  // beside the per-step kernels: disjoint masses
+            CK(cudaEventRecord(s->ev_fork, s->stream), "launch resident tiles");
+            CK(cudaStreamWaitEvent(s->side_stream, s->ev_fork, 0), "launch resident tiles");
+            CK(tg::launch_tile_resident(s->prec, s->args, s->rtargs, s->rt_mpt, s->rt_threads, s->rt_smem,
+                                        s->parity, nsteps, 1, s->side_stream),
+               "launch resident tiles");
+            CK(cudaEventRecord(s->ev_join, s->side_stream), "launch resident tiles");
+            joined = false;
+        }
+    }
     if (s->args.ntiles == 0) {
         s->parity ^= (int)(nsteps & 1);
         for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
@@ -1190,19 +1319,25 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
         return TITAN_GB300_OK;
     }
     const int P = s->passes();
-    int64_t rem = nsteps - 1;
-    while (rem > 0) {
-        int len = (int)std::min<int64_t>(rem, kChunk);
-        cudaGraphExec_t g = get_graph(s, len, s->parity, e);
-        if (!g) return s->cuda_fail(e, "build step graph");
-        CK(cudaGraphLaunch(g, s->stream), "launch step graph");
-        s->parity ^= ((len * P) & 1);
-        rem -= len;
-    }
-    for (int q = 0; q < P; q++) {  // the last step also writes the accelerations
-        CK(s->launch(s->parity, q == P - 1, q), "launch step");
-        s->parity ^= 1;
-    }
+    const int rc = [&]() -> int {
+        int64_t rem = nsteps - 1;
+        while (rem > 0) {
+            int len = (int)std::min<int64_t>(rem, kChunk);
+            cudaGraphExec_t g = get_graph(s, len, s->parity, e);
+            if (!g) return s->cuda_fail(e, "build step graph");
+            CK(cudaGraphLaunch(g, s->stream), "launch step graph");
+            s->parity ^= ((len * P) & 1);
+            rem -= len;
+        }
+        for (int q = 0; q < P; q++) {  // the last step also writes the accelerations
+            CK(s->launch(s->parity, q == P - 1, q), "launch step");
+            s->parity ^= 1;
+        }
+        return TITAN_GB300_OK;
+    }();
+    // later work on the handle's stream sees the resident tiles' results
+    if (!joined) CK(cudaStreamWaitEvent(s->stream, s->ev_join, 0), "join resident tiles");
+    if (rc) return rc;
     if (P == 2) {
         const double h = 0.5 * s->dt;
         for (int64_t i = 0; i < nsteps; i++) {  // src/sim.cu:1574-1583

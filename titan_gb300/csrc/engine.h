@@ -136,6 +136,17 @@ struct ResArgs {
     int32_t cap;                   // masses per bin (shared memory holds 2 * cap records)
 };
 
+// Resident tiles (resident_tiles.cu): tiles with no halo (every spring of
+// their masses has both ends in the tile: a whole body, or a part of one
+// that no spring joins to the rest) stepped by one CTA each for all steps
+// of a launch, with the per-step kernels' two phases in shared memory.
+struct TileResArgs {
+    const TileInfo *tiles;  // the resident tiles
+    const double *t0;       // T of the launch's first step (a copy taken before per-step kernels run beside it)
+    int32_t ntiles;
+    int32_t stage;          // 1: slab, actuation and incidence records staged in shared memory once per launch
+};
+
 // Per-mass gather / scatter between caller order and tiled order.
 struct XferArgs {
     const int32_t *old2new;
@@ -211,6 +222,18 @@ cudaError_t resident_prepare(int precision, int mpt, size_t smem);
 int resident_ctas_per_sm(int precision, int mpt, int threads, size_t smem);
 cudaError_t launch_resident(int precision, const StepArgs &a, const ResArgs &r, int ctas, int threads, int parity,
                             int64_t nsteps, int write_acc, int write_time, cudaStream_t s);
+// The device time record advanced by nsteps additions of dt, for launches
+// with no per-step tiles.
+cudaError_t launch_advance_time(const StepArgs &a, int parity, int64_t nsteps, cudaStream_t s);
+// Resident tiles: shared memory of one tile (state twice, force slots and
+// the zero slot, heavy sums, and with stage the tile's slab, actuation and
+// incidence records; launch parameters first), and the launch (masses per
+// thread = ceil(largest tile / threads) at most kResMaxMpt).
+size_t tile_resident_smem_bytes(int precision, const TileInfo &ti, int stage);
+cudaError_t tile_resident_prepare(int precision, int mpt, int stage, size_t smem);
+int tile_resident_ctas_per_sm(int precision, int mpt, int stage, int threads, size_t smem);
+cudaError_t launch_tile_resident(int precision, const StepArgs &a, const TileResArgs &r, int mpt, int threads,
+                                 size_t smem, int parity, int64_t nsteps, int write_acc, cudaStream_t s);
 cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
 // float positions of all a.count masses in caller order into out (device)
 cudaError_t launch_export_f32(int precision, const XferArgs &a, float *out, cudaStream_t s);

@@ -236,11 +236,12 @@ cudaError_t launch_resident(int precision, const StepArgs &a, const ResArgs &r, 
         e = cudaLaunchKernel(res_kernel(precision, mpt), dim3(ctas), dim3(threads), args, smem, s);
         if (e != cudaSuccess) return e;
     }
-    if (write_time) {
-        k_advance_time<<<1, 1, 0, s>>>(a.tbuf, parity, nsteps, a.prm);
-        return cudaGetLastError();
-    }
-    return cudaSuccess;
+    return write_time ? launch_advance_time(a, parity, nsteps, s) : cudaSuccess;
+}
+
+cudaError_t launch_advance_time(const StepArgs &a, int parity, int64_t nsteps, cudaStream_t s) {
+    k_advance_time<<<1, 1, 0, s>>>(a.tbuf, parity, nsteps, a.prm);
+    return cudaGetLastError();
 }
 
 }  // namespace tg
