@@ -54,3 +54,19 @@ def test_poisson_arrivals_complete():
     srv.close()
     assert stats["requests"] == 40
     assert all(rec["latency_ms"] > 0 for rec in recs.values())
+
+
+def test_small_designs_run_as_one_resident_tile():
+    """A design that fits one CTA's shared memory is served as one
+    halo-free tile (resident-tile launches); a larger one on the per-step
+    kernels; results as when run alone."""
+    reqs = [{"id": 0, "arrival_s": 0.0, "side": 7, "steps": 120, "seed": 5},
+            {"id": 1, "arrival_s": 0.0, "side": 12, "steps": 60, "seed": 6}]
+    srv = serving.RolloutServer(tg.FP32C)
+    recs, _ = srv.run(reqs, keep_results=True)
+    (e7,), (e12,) = srv.pool[7], srv.pool[12]
+    assert e7.resident_info()["active"] == 2 and e7.plan_info()["tiles"] == 1
+    assert e12.resident_info()["active"] == 0
+    for r in reqs:
+        assert np.array_equal(recs[r["id"]]["pos"], alone(r["side"], r["seed"], r["steps"], tg.FP32C))
+    srv.close()

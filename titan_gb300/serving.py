@@ -15,6 +15,9 @@ per process):
     state, spring parameters and clock (no reallocation, no replanning, the
     CUDA graphs stay cached), and the first engine of a design takes its
     plan from a host-planned template (adopt_plan);
+  * a design small enough for one CTA's shared memory runs as one tile of
+    its own size: a halo-free tile, stepped for the whole rollout by one
+    resident-tile launch (one CTA, no per-step launches);
   * a request's result is the same bits whether it runs alone or among
     others: its engine's arithmetic depends only on its own scene.
 """
@@ -25,18 +28,32 @@ import time
 
 import numpy as np
 
-from . import FP32C, Sim
+from . import FP32, FP32C, FP64, Sim
 from . import workloads as wl
+
+_SMEM_PER_CTA = 227 * 1024
+
+
+def resident_tile_fits(precision, masses, springs):
+    """Whether a body of this size fits one resident tile: launch parameters,
+    two state records per mass and a force slot per spring (plus the zero
+    slot) in one CTA's shared memory."""
+    rec = 32 if precision == FP32 else 48
+    slot = 32 if precision == FP64 else 16
+    return 2016 + 2 * masses * rec + (springs + 1) * slot + 64 <= _SMEM_PER_CTA and masses <= 2048
 
 
 class RolloutServer:
     def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_active=256, pool_per_design=64,
-                 small_masses=50000):
-        """small_masses: scenes below this size run the per-tile kernel with
-        128-mass tiles (a few CTAs per SM, so that many small rollouts share
-        the SMs); larger ones the automatic kernel (one persistent CTA per
-        SM).  0 disables the split."""
+                 small_masses=50000, resident_tiles=True):
+        """Designs that fit one CTA's shared memory run as one resident tile;
+        small_masses: larger scenes below this size run the per-tile kernel
+        with 128-mass tiles (a few CTAs per SM, so that many small rollouts
+        share the SMs); larger ones the automatic kernel (one persistent CTA
+        per SM).  0 disables the split.  resident_tiles=False keeps every
+        design on the per-step kernels."""
         self.precision = precision
+        self.resident_tiles = resident_tiles
         self.small_masses = small_masses
         self.device = device
         self.budget = float(hbm_budget_bytes)
@@ -65,8 +82,13 @@ class RolloutServer:
                                 omega=sc["omega"], amp=sc["amp"], phase=sc["phase"])
             e.set_time(0.0)
             return e
-        small = sc["pos"].shape[0] < self.small_masses
-        kernel, tile = (1, 128) if small else (0, 0)
+        n, ns = sc["pos"].shape[0], sc["left"].size
+        if self.resident_tiles and resident_tile_fits(self.precision, n, ns):
+            kernel, tile = 0, max(32, n)  # one halo-free tile: a resident-tile launch per rollout
+        elif n < self.small_masses:
+            kernel, tile = 1, 128
+        else:
+            kernel, tile = 0, 0
         if side not in self.templates:
             t = Sim(self.precision, self.device)
             wl.load(t, sc, start=False, kernel=kernel)
