@@ -181,8 +181,10 @@ int titan_gb300_set_occupancy(titan_gb300_sim *sim, int min_ctas_per_sm);
  * start(). */
 int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
 
-/* After start(): out[0] kernel form in use (1, 2 or 3), out[1] CTAs per launch,
- * out[2] threads per CTA, out[3] dynamic shared memory per CTA (bytes). */
+/* After start(): out[0] kernel form of the per-step launches (1 to 4; 5
+ * when resident tiles carry the whole scene and no per-step kernel runs),
+ * out[1] CTAs per launch, out[2] threads per CTA, out[3] dynamic shared
+ * memory per CTA (bytes) -- of the resident-tile launch for form 5. */
 int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
 
 /* Batched bodies (no reference counterpart: the reference runs one scene

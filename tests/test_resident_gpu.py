@@ -188,6 +188,7 @@ def test_automatic_resident_tiles_choice():
     small = wl.config1(contact=True)
     s = wl.make_sim(small, tg.FP32C)
     assert s.resident_info()["active"] == 2 and s.plan_info()["tiles"] == 1
+    assert s.kernel_info()["kernel"] == "resident-tiles" and s.kernel_info()["ctas"] == 1
     s.close()
     s = wl.make_sim(small, tg.FP32C, kernel=1)  # an explicit kernel form: per-step kernels
     assert s.resident_info()["active"] == 0
@@ -214,3 +215,20 @@ def test_set_integrator_leaves_resident_tiles_bitwise():
         assert s.resident_info()["active"] == 0
         out.append(s.get_state(acc=True, T=True))
     assert_same(*out)
+
+
+@pytest.mark.parametrize("precision", [tg.FP64, tg.FP32C])
+def test_resident_tiles_many_tiles_bitwise(precision):
+    """More halo-free tiles than SMs (unstaged records, CTAs of 128
+    threads) and fewer (staged records, wider CTAs): both bit-identical to
+    the per-step kernels."""
+    sc = batch(nbodies=200, seed=18, side_range=(3, 5), passive=False)
+    chunks = [2, 97, 101]
+    s1, a = run(sc, chunks, precision, resident=(2, 0, 0))
+    assert s1.resident_info()["bins"] == 200
+    s2, b = run(sc, chunks, precision, resident=(0, 0, 0))
+    assert_same(a, b)
+    few = batch(nbodies=8, seed=19, side_range=(3, 5), passive=False)
+    s3, c = run(few, chunks, precision, resident=(2, 0, 0))
+    s4, d = run(few, chunks, precision, resident=(0, 0, 0))
+    assert_same(c, d)

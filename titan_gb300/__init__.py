@@ -290,7 +290,7 @@ class Sim:
     def kernel_info(self) -> dict:
         out = np.zeros(4, np.int64)
         self._check(self._L.titan_gb300_kernel_info(self._h, _ptr(out, ctypes.c_int64)), "kernel_info")
-        names = {1: "per-tile", 2: "pipelined", 3: "per-tile-async", 4: "warp-specialised"}
+        names = {1: "per-tile", 2: "pipelined", 3: "per-tile-async", 4: "warp-specialised", 5: "resident-tiles"}
         return {"kernel": names.get(int(out[0]), "per-tile"), "ctas": int(out[1]), "threads": int(out[2]),
                 "smem_bytes": int(out[3])}
 

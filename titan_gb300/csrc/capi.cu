@@ -942,6 +942,13 @@ int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
 
 int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
     if (!s || !out) return TITAN_GB300_EINVAL;
+    if (s->use_rtiles && s->args.ntiles == 0) {
+        out[0] = 5;
+        out[1] = s->rtargs.ntiles;
+        out[2] = s->rt_threads;
+        out[3] = (int64_t)s->rt_smem;
+        return TITAN_GB300_OK;
+    }
     out[0] = s->use_pipe ? 2 : (s->use_async ? 3 : (s->use_ws ? 4 : 1));
     out[1] = (s->use_pipe || s->use_ws) ? s->ctas : s->args.ntiles;
     out[2] = s->threads;
