@@ -27,6 +27,158 @@ bool actuated(const PlanInput &in, int64_t s) {
     return in.type && (in.type[s] == 2 || in.type[s] == 3);
 }
 
+
+// Orders one part of a tile's slab (entries given with their left and right
+// state-record slots) so that each aligned group of eight entries -- the
+// eight lanes of one quarter-warp, whose 16-byte shared-memory loads of the
+// endpoint records are served together -- reads its records from distinct
+// bank groups where it can.  A 48-byte record at slot x puts its k-th
+// 16-byte piece in bank group (3x + k) mod 8 and a 32-byte one in (2x + k)
+// mod 8, so two entries of a group conflict when their left (or right) slots
+// differ but agree mod 8 (48-byte records) or mod 4 (32-byte records; at
+// most two distinct slots per residue are then unavoidable).  Equal slots
+// are one broadcast and never conflict.  The part starts `lead` entries
+// into a group whose earlier entries (the previous part's last ones) have
+// slots lead_ls / lead_rs.  Greedy, in spring order: each group takes the
+// first remaining entries within a window that add no conflict, then fills
+// up with the first remaining ones.  The order of an entry in the slab
+// changes no result: each mass sums its entries' forces in its incidence
+// order.
+void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const std::vector<uint32_t> &rs,
+                int record_bytes, const uint32_t *lead_ls, const uint32_t *lead_rs, int lead) {
+    const int64_t n = (int64_t)v.size();
+    const int mod = record_bytes == 32 ? 4 : 8, cap = 8 / mod;
+    constexpr int kWindow = 64;
+    // unused entries as a doubly linked list in spring order (n: the end)
+    std::vector<int64_t> nx(n + 1), pv(n + 1);
+    for (int64_t q = 0; q <= n; q++) {
+        nx[q] = q + 1;
+        pv[q] = q - 1;
+    }
+    int64_t head = n > 0 ? 0 : n;
+    auto take = [&](int64_t q) {
+        if (pv[q] >= 0) nx[pv[q]] = nx[q];
+        else head = nx[q];
+        if (nx[q] <= n) pv[nx[q]] = pv[q];
+    };
+    std::vector<int64_t> out;
+    out.reserve(n);
+    bool first = true;
+    while ((int64_t)out.size() < n) {
+        uint32_t lsl[8][2], rsl[8][2];
+        int lcnt[8] = {0}, rcnt[8] = {0};
+        auto fits = [&](const uint32_t (*tab)[2], const int *cnt, uint32_t x) {
+            const int r = (int)(x % (uint32_t)mod);
+            for (int q = 0; q < cnt[r]; q++)
+                if (tab[r][q] == x) return true;
+            return cnt[r] < cap;
+        };
+        auto add = [&](uint32_t (*tab)[2], int *cnt, uint32_t x) {
+            const int r = (int)(x % (uint32_t)mod);
+            for (int q = 0; q < cnt[r]; q++)
+                if (tab[r][q] == x) return;
+            if (cnt[r] < cap) tab[r][cnt[r]++] = x;
+        };
+        int taken = 0;
+        if (first) {
+            for (int q = 0; q < lead; q++) {
+                add(lsl, lcnt, lead_ls[q]);
+                add(rsl, rcnt, lead_rs[q]);
+            }
+            taken = lead;
+            first = false;
+        }
+        int seen = 0;
+        for (int64_t q = head; q < n && taken < 8 && seen < kWindow;) {
+            const int64_t nq = nx[q];
+            seen++;
+            if (fits(lsl, lcnt, ls[q]) && fits(rsl, rcnt, rs[q])) {
+                add(lsl, lcnt, ls[q]);
+                add(rsl, rcnt, rs[q]);
+                take(q);
+                out.push_back(v[q]);
+                taken++;
+            }
+            q = nq;
+        }
+        while (head < n && taken < 8) {
+            const int64_t q = head;
+            take(q);
+            out.push_back(v[q]);
+            taken++;
+        }
+    }
+    v.swap(out);
+}
+
+// Permutes the entries inside each aligned group of eight slab positions
+// (never across the actuated / non-actuated boundary), which keeps the
+// grouping above, so that the force slots one quarter-warp gathers at one
+// incidence position -- the j-th codes of eight consecutive masses, 16-byte
+// loads of slots at bank group (slot mod 8) -- fall in distinct bank groups
+// where they can.  Greedy per group: the entries with the most gather
+// references first, each to the free position whose residue the entry's
+// (quarter-warp, j) sets use least.  elocal is scratch (spring -> position).
+void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64_t lo, int64_t hi,
+                    const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold,
+                    std::vector<int32_t> &elocal) {
+    std::vector<int64_t> seq(act);
+    seq.insert(seq.end(), rest.begin(), rest.end());
+    const int64_t ne = (int64_t)seq.size(), na = (int64_t)act.size(), nm = hi - lo;
+    if (ne <= 1) return;
+    for (int64_t p = 0; p < ne; p++) elocal[seq[p]] = (int32_t)p;
+    int64_t maxd = 1;
+    for (int64_t m = lo; m < hi; m++) {
+        const int64_t d = ip[m + 1] - ip[m];
+        if (d <= heavy_threshold) maxd = std::max(maxd, d);
+    }
+    // the (quarter-warp, incidence position) sets each entry belongs to
+    std::vector<int32_t> k0(ne, -1), k1(ne, -1);
+    for (int64_t m = lo; m < hi; m++) {
+        const int64_t d = ip[m + 1] - ip[m];
+        if (d > heavy_threshold) continue;
+        for (int64_t j = 0; j < d; j++) {
+            const int64_t p = elocal[isp[ip[m] + j]];
+            const int32_t key = (int32_t)(((m - lo) >> 3) * maxd + j);
+            (k0[p] < 0 ? k0[p] : k1[p]) = key;
+        }
+    }
+    std::vector<uint8_t> cnt((size_t)(((nm + 7) >> 3) * maxd * 8), 0);
+    std::vector<int64_t> out(seq);
+    for (int64_t b0 = 0; b0 < ne; b0 += 8) {
+        const int64_t b1 = std::min<int64_t>(b0 + 8, ne);
+        for (int side = 0; side < 2; side++) {
+            const int64_t s0 = side == 0 ? b0 : std::max(b0, na), s1 = side == 0 ? std::min(b1, na) : b1;
+            if (s1 - s0 <= 0) continue;
+            int64_t ord[8];  // the entries of positions s0..s1-1 (by their position in seq)
+            int n8 = 0;
+            for (int64_t x = s0; x < s1; x++) ord[n8++] = x;
+            std::stable_sort(ord, ord + n8, [&](int64_t x, int64_t y) {
+                return (k0[x] >= 0) + (k1[x] >= 0) > (k0[y] >= 0) + (k1[y] >= 0);
+            });
+            bool taken[8] = {false};
+            for (int q = 0; q < n8; q++) {
+                const int64_t x = ord[q];
+                int best = -1, bestc = 1 << 30;
+                for (int64_t p = s0; p < s1; p++) {
+                    if (taken[p - s0]) continue;
+                    const int r = (int)(p & 7);
+                    const int c = (k0[x] >= 0 ? cnt[(size_t)k0[x] * 8 + r] : 0) +
+                                  (k1[x] >= 0 ? cnt[(size_t)k1[x] * 8 + r] : 0);
+                    if (c < bestc) bestc = c, best = (int)(p - s0);
+                }
+                taken[best] = true;
+                const int r = (int)((s0 + best) & 7);
+                if (k0[x] >= 0) cnt[(size_t)k0[x] * 8 + r]++;
+                if (k1[x] >= 0) cnt[(size_t)k1[x] * 8 + r]++;
+                out[s0 + best] = seq[x];
+            }
+        }
+    }
+    act.assign(out.begin(), out.begin() + na);
+    rest.assign(out.begin() + na, out.end());
+}
+
 }  // namespace
 
 std::string build_plan(const PlanInput &in, Plan &P) {
@@ -180,7 +332,8 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 work.emplace_front(lo, mid);
                 continue;
             }
-            // commit tile (slab: actuated entries first, each part in spring order)
+            // commit tile (slab: actuated entries first, each part in spring
+            // order, then grouped for conflict-free endpoint loads)
             std::sort(ents_act.begin(), ents_act.end());
             std::sort(ents.begin(), ents.end());
             std::sort(halo.begin(), halo.end());
@@ -189,6 +342,31 @@ std::string build_plan(const PlanInput &in, Plan &P) {
             auto slot = [&](int32_t x) -> uint32_t {
                 return (x >= lo && x < hi) ? (uint32_t)(x - lo) : (uint32_t)hslot[x];
             };
+            {
+                // the non-actuated part continues the actuated part's last group
+                uint32_t lead_ls[8], lead_rs[8];
+                int lead = 0;
+                for (auto *v : {&ents_act, &ents}) {
+                    std::vector<uint32_t> ls(v->size()), rs(v->size());
+                    for (size_t q = 0; q < v->size(); q++) {
+                        ls[q] = slot(L[(*v)[q]]);
+                        rs[q] = slot(R[(*v)[q]]);
+                    }
+                    bank_order(*v, ls, rs, in.slot_bytes, lead_ls, lead_rs, lead);
+                    // the open group after this part: its last (lead + size) % 8
+                    // entries of the carried ones followed by this part's
+                    std::vector<uint32_t> cl(lead_ls, lead_ls + lead), cr(lead_rs, lead_rs + lead);
+                    for (int64_t sp : *v) {
+                        cl.push_back(slot(L[sp]));
+                        cr.push_back(slot(R[sp]));
+                    }
+                    const int tail = (int)(cl.size() % 8);
+                    std::copy(cl.end() - tail, cl.end(), lead_ls);
+                    std::copy(cr.end() - tail, cr.end(), lead_rs);
+                    lead = tail;
+                }
+            }
+            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold, elocal);
             int32_t e = 0;
             for (auto *v : {&ents_act, &ents})
                 for (int64_t s : *v) {
