@@ -178,10 +178,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                 issue_chunks(st + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), ib, &full[s]);
                 issue_chunks(st, in + (int64_t)ti.mass_off * kRec, sb, &full[s]);
             }
+            // halo records, one per lane at a time (the producer issues for
+            // every stage: its instruction count is on the critical path)
             const int32_t *ix = idxbuf + (k & 1) * L.idx_words;
-            for (int q = lane; q < ti.nh * kChunks; q += 32) {
-                const int h = q / kChunks, c = q - h * kChunks;
-                cp_async16(st + (int64_t)(ti.nm + h) * kRec + 16 * c, in + (int64_t)ix[h] * kRec + 16 * c);
+            for (int h = lane; h < ti.nh; h += 32) {
+                const uint8_t *src = in + (int64_t)ix[h] * kRec;
+                uint8_t *dst = st + (int64_t)(ti.nm + h) * kRec;
+#pragma unroll
+                for (int c = 0; c < kChunks; c++) cp_async16(dst + 16 * c, src + 16 * c);
             }
             cp_async_arrive(&full[s]);
             __syncwarp();  // every lane has read ring entry k & 1
