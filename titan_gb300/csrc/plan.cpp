@@ -118,15 +118,31 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
 // loads of slots at bank group (slot mod 8) -- fall in distinct bank groups
 // where they can.  Greedy per group: the entries with the most gather
 // references first, each to the free position whose residue the entry's
-// (quarter-warp, j) sets use least.  elocal is scratch (spring -> position).
+// (quarter-warp, j) sets use least.
 void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64_t lo, int64_t hi,
-                    const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold,
-                    std::vector<int32_t> &elocal) {
+                    const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold) {
     std::vector<int64_t> seq(act);
     seq.insert(seq.end(), rest.begin(), rest.end());
     const int64_t ne = (int64_t)seq.size(), na = (int64_t)act.size(), nm = hi - lo;
     if (ne <= 1) return;
-    for (int64_t p = 0; p < ne; p++) elocal[seq[p]] = (int32_t)p;
+    // spring -> position of this tile, in a small open-addressing table
+    // (the global spring-indexed array would be read at scattered places)
+    int64_t hcap = 16;
+    while (hcap < 2 * ne) hcap <<= 1;
+    std::vector<int64_t> hkey((size_t)hcap, -1);
+    std::vector<int32_t> hval((size_t)hcap, 0);
+    auto hslot = [&](int64_t sp) {
+        uint64_t h = ((uint64_t)sp * 0x9E3779B97F4A7C15ULL) >> 20;
+        for (;; h++) {
+            const size_t q = (size_t)(h & (uint64_t)(hcap - 1));
+            if (hkey[q] == sp || hkey[q] < 0) return q;
+        }
+    };
+    for (int64_t p = 0; p < ne; p++) {
+        const size_t q = hslot(seq[p]);
+        hkey[q] = seq[p];
+        hval[q] = (int32_t)p;
+    }
     int64_t maxd = 1;
     for (int64_t m = lo; m < hi; m++) {
         const int64_t d = ip[m + 1] - ip[m];
@@ -138,7 +154,7 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
         const int64_t d = ip[m + 1] - ip[m];
         if (d > heavy_threshold) continue;
         for (int64_t j = 0; j < d; j++) {
-            const int64_t p = elocal[isp[ip[m] + j]];
+            const int64_t p = hval[hslot(isp[ip[m] + j])];
             const int32_t key = (int32_t)(((m - lo) >> 3) * maxd + j);
             (k0[p] < 0 ? k0[p] : k1[p]) = key;
         }
@@ -153,9 +169,10 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
             int64_t ord[8];  // the entries of positions s0..s1-1 (by their position in seq)
             int n8 = 0;
             for (int64_t x = s0; x < s1; x++) ord[n8++] = x;
-            std::stable_sort(ord, ord + n8, [&](int64_t x, int64_t y) {
-                return (k0[x] >= 0) + (k1[x] >= 0) > (k0[y] >= 0) + (k1[y] >= 0);
-            });
+            // most gather references first (stable insertion sort of <= 8)
+            auto refs = [&](int64_t x) { return (k0[x] >= 0) + (k1[x] >= 0); };
+            for (int q = 1; q < n8; q++)
+                for (int r = q; r > 0 && refs(ord[r]) > refs(ord[r - 1]); r--) std::swap(ord[r], ord[r - 1]);
             bool taken[8] = {false};
             for (int q = 0; q < n8; q++) {
                 const int64_t x = ord[q];
@@ -366,7 +383,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     lead = tail;
                 }
             }
-            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold, elocal);
+            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold);
             int32_t e = 0;
             for (auto *v : {&ents_act, &ents})
                 for (int64_t s : *v) {
