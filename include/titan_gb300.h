@@ -254,6 +254,15 @@ double titan_gb300_time(const titan_gb300_sim *sim);
 /* Device memory held by the handle (bytes), for admission control. */
 int64_t titan_gb300_device_bytes(const titan_gb300_sim *sim);
 
+/* Page-locked host memory (cudaMallocHost) for state buffers: get_state,
+ * get_masses and set_mass_state move a page-locked caller buffer by DMA
+ * directly, any other buffer through the handle's own page-locked staging
+ * copy.  host_alloc returns NULL on failure; host_free accepts NULL.
+ * Extension (the reference moves state through its own pinned-less
+ * cudaMemcpy, src/sim.cu:588-764). */
+void *titan_gb300_host_alloc(size_t bytes);
+void titan_gb300_host_free(void *p);
+
 /* Number of steps run since start(). */
 int64_t titan_gb300_steps(const titan_gb300_sim *sim);
 

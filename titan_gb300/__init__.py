@@ -16,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["FP64", "FP32", "FP32C", "TitanError", "Sim", "lattice", "lattice_springs", "lib",
+__all__ = ["FP64", "FP32", "FP32C", "TitanError", "Sim", "lattice", "lattice_springs", "lib", "pinned_empty",
            "library_path"]
 
 FP64, FP32, FP32C = 0, 1, 2
@@ -79,6 +79,8 @@ _SIGS = {
     "titan_gb300_time": (ctypes.c_double, [_P]),
     "titan_gb300_set_time": (ctypes.c_int, [_P, ctypes.c_double]),
     "titan_gb300_device_bytes": (ctypes.c_int64, [_P]),
+    "titan_gb300_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "titan_gb300_host_free": (None, [ctypes.c_void_p]),
     "titan_gb300_steps": (ctypes.c_int64, [_P]),
     "titan_gb300_get_state": (ctypes.c_int, [_P, _D, _D, _D, _D]),
     "titan_gb300_get_masses": (ctypes.c_int, [_P, ctypes.c_int64, _I64, _D, _D, _D, _D]),
@@ -136,6 +138,32 @@ def _i64(a):
 
 def _u8(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.uint8)
+
+
+class _PinnedBlock:
+    """Page-locked host memory (titan_gb300_host_alloc), freed with the last
+    array that views it."""
+
+    def __init__(self, shape, dtype):
+        self.dtype = np.dtype(dtype)
+        self.shape = tuple(int(x) for x in shape)
+        nbytes = int(np.prod(self.shape, dtype=np.int64)) * self.dtype.itemsize
+        self.ptr = lib().titan_gb300_host_alloc(max(nbytes, 1))
+        if not self.ptr:
+            raise MemoryError(f"page-locked host allocation of {nbytes} bytes failed")
+        self.__array_interface__ = {"data": (self.ptr, False), "shape": self.shape, "typestr": self.dtype.str,
+                                    "version": 3}
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().titan_gb300_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """An uninitialised array in page-locked host memory: get_state /
+    set_mass_state move it by DMA directly (no staging copy)."""
+    return np.asarray(_PinnedBlock(shape, dtype))
 
 
 def lattice_springs(nx: int, ny: int, nz: int) -> int:

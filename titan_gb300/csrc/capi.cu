@@ -204,6 +204,43 @@ namespace {
         if (e_ != cudaSuccess) return s->cuda_fail(e_, what); \
     } while (0)
 
+// Whether a caller's host buffer is page-locked (cudaMallocHost or
+// cudaHostRegister): such buffers are copied by DMA directly, without the
+// staging copy through the handle's own pinned buffer.
+bool host_pinned(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the error state the failed query left
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// memcpy of large host buffers split over a few threads (the staging copies
+// of whole-scene state are tens of MB; one core copies them at a fraction of
+// the host memory bandwidth).
+void par_memcpy(void *dst, const void *src, size_t bytes) {
+    constexpr size_t kPiece = 8u << 20;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>(std::min<size_t>(8, hw), (bytes + kPiece - 1) / kPiece);
+    if (nt <= 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = (bytes / nt + 63) & ~size_t(63);
+    std::vector<std::thread> th;
+    for (size_t q = 1; q < nt; q++) {
+        const size_t o = q * per;
+        if (o >= bytes) break;
+        th.emplace_back([=] {
+            std::memcpy(static_cast<uint8_t *>(dst) + o, static_cast<const uint8_t *>(src) + o, std::min(per, bytes - o));
+        });
+    }
+    std::memcpy(dst, src, std::min(per, bytes));
+    for (auto &t : th) t.join();
+}
+
 uint8_t mass_flags(const titan_gb300_sim *s, int64_t i) {
     uint8_t f = 0;
     if (!s->fixed.empty() && s->fixed[i]) f |= tg::MF_FIXED;
@@ -1437,6 +1474,19 @@ double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }
 
 int64_t titan_gb300_device_bytes(const titan_gb300_sim *s) { return s ? (int64_t)s->mem.total : 0; }
 
+void *titan_gb300_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void titan_gb300_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
 int titan_gb300_set_time(titan_gb300_sim *s, double T) {
     if (!s) return TITAN_GB300_EINVAL;
     s->T = T;
@@ -1471,15 +1521,24 @@ int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx
     x.pos = pos ? s->d_xfer : nullptr;
     x.vel = vel ? s->d_xfer + 3 * count : nullptr;
     x.accout = acc ? s->d_xfer + 6 * count : nullptr;
+    // only the requested arrays come back: into a pinned caller buffer by
+    // DMA directly, else through the handle's pinned staging buffer
+    double *outs[3] = {pos, vel, acc};
+    bool direct[3] = {false, false, false};
     if (pos || vel || acc) {
         CK(tg::launch_gather(s->prec, x, s->stream), "gather");
-        CK(cudaMemcpyAsync(s->h_xfer, s->d_xfer, 9 * count * 8, cudaMemcpyDeviceToHost, s->stream), "download");
+        for (int q = 0; q < 3; q++) {
+            if (!outs[q]) continue;
+            direct[q] = host_pinned(outs[q]);
+            double *dst = direct[q] ? outs[q] : s->h_xfer + 3 * q * count;
+            CK(cudaMemcpyAsync(dst, s->d_xfer + 3 * q * count, 3 * count * 8, cudaMemcpyDeviceToHost, s->stream),
+               "download");
+        }
     }
     CK(cudaStreamSynchronize(s->stream), "download");
     if (int rc = check_kernel_error(s)) return rc;
-    if (pos) std::memcpy(pos, s->h_xfer, 3 * count * 8);
-    if (vel) std::memcpy(vel, s->h_xfer + 3 * count, 3 * count * 8);
-    if (acc) std::memcpy(acc, s->h_xfer + 6 * count, 3 * count * 8);
+    for (int q = 0; q < 3; q++)
+        if (outs[q] && !direct[q]) par_memcpy(outs[q], s->h_xfer + 3 * q * count, 3 * count * 8);
     if (T) mass_times(s, idx, count, T);
     return TITAN_GB300_OK;
 }
@@ -1565,9 +1624,19 @@ int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t 
             CK(cudaMemcpyAsync(s->d_idx, idx, count * 8, cudaMemcpyHostToDevice, s->stream), "upload index");
             x.idx = s->d_idx;
         }
-        if (pos) std::memcpy(s->h_xfer, pos, 3 * count * 8);
-        if (vel) std::memcpy(s->h_xfer + 3 * count, vel, 3 * count * 8);
-        CK(cudaMemcpyAsync(s->d_xfer, s->h_xfer, 6 * count * 8, cudaMemcpyHostToDevice, s->stream), "upload");
+        // a pinned caller buffer goes up by DMA directly, else through the
+        // handle's pinned staging buffer
+        const double *ins[2] = {pos, vel};
+        for (int q = 0; q < 2; q++) {
+            if (!ins[q]) continue;
+            const double *src = ins[q];
+            if (!host_pinned(src)) {
+                par_memcpy(s->h_xfer + 3 * q * count, src, 3 * count * 8);
+                src = s->h_xfer + 3 * q * count;
+            }
+            CK(cudaMemcpyAsync(s->d_xfer + 3 * q * count, src, 3 * count * 8, cudaMemcpyHostToDevice, s->stream),
+               "upload");
+        }
         x.ipos = pos ? s->d_xfer : nullptr;
         x.ivel = vel ? s->d_xfer + 3 * count : nullptr;
         CK(tg::launch_scatter(s->prec, x, s->stream), "scatter");
