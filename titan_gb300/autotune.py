@@ -19,8 +19,8 @@ from . import workloads as wl
 # (kernel form, tile masses, threads per CTA); form 4 = warp-specialised
 # (threads = consumer threads), 3 = per-tile with asynchronous staging,
 # 1 = per-tile
-CANDIDATES_F32 = [(4, 192, 448), (4, 176, 448), (4, 160, 448), (4, 192, 384), (3, 256, 256), (1, 256, 256),
-                  (1, 128, 128)]
+CANDIDATES_F32 = [(4, 208, 448), (4, 192, 448), (4, 176, 448), (4, 160, 448), (4, 112, 448), (3, 256, 256),
+                  (1, 256, 256), (1, 128, 128)]
 CANDIDATES_F64 = [(1, 128, 128), (1, 64, 128), (3, 128, 128), (1, 128, 256)]
 
 

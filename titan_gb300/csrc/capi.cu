@@ -150,6 +150,7 @@ struct titan_gb300_sim {
     // used by the first start() only
     bool plan_adopted = false;
     int plan_tile = 0;  // tile size the current plan was built with
+    int plan_req = 0;   // tile size requested for it (0: the default)
 
     cudaError_t launch(int parity, int write_acc, int stage = 0) {
         if (args.ntiles == 0) return cudaSuccess;
@@ -423,6 +424,11 @@ T *dev_copy(titan_gb300_sim *s, const std::vector<T> &v, cudaError_t &e) {
     return e == cudaSuccess ? p : nullptr;
 }
 
+// default tile of the warp-specialised form, and its fallback when two
+// stages of the default's tiles do not fit one SM's shared memory
+constexpr int kWsDefaultTile = 208;
+constexpr int kWsFallbackTile = 192;
+
 tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     tg::PlanInput in;
     in.n = s->n;
@@ -434,11 +440,12 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    // default tile: 128 masses in FP64; in the FP32 forms 192 for the
-    // warp-specialised kernel (two stages fit one SM's shared memory) and 256
-    // for the per-tile forms (measured fastest on GB300, see profiles/)
+    // default tile: 128 masses in FP64; in the FP32 forms 208 for the
+    // warp-specialised kernel (two stages fit one SM's shared memory; 192
+    // where they would not, plan_scene) and 256 for the per-tile forms
+    // (measured fastest on GB300, see profiles/)
     const bool ws = s->kernel_req == 0 || s->kernel_req == 4;
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : (ws ? 192 : 256));
+    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 128 : (ws ? kWsDefaultTile : 256));
     in.heavy_threshold = 96;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)
@@ -476,33 +483,8 @@ int resident_cap(const titan_gb300_sim *s) {
     return std::min(lim, (cap + 31) & ~31);
 }
 
-// Builds the plan and all device buffers; positions/velocities come from the
-// host mirror.  Keeps T / steps.
-int build_device(titan_gb300_sim *s) {
-    s->free_device();
-    tg::PlanInput in = plan_input(s, s->tile_masses);
-    const size_t rs = s->rsize();
-    if (s->plan_adopted && !s->started && s->plan_tile == in.tile_cap) {
-        s->plan_adopted = false;  // the adopted plan serves this first start
-    } else {
-        s->plan_adopted = false;
-        std::string why = tg::build_plan(in, s->plan);
-        if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
-        s->plan_tile = in.tile_cap;
-    }
-    const tg::Plan &P = s->plan;
-    s->threads = s->threads_req > 0 ? s->threads_req : std::max(128, std::min(512, ((P.max_nm + 31) / 32) * 32));
-    s->npad = ((s->n + 127) / 128) * 128;
-    const int64_t np = s->npad;
-    auto &a = s->args;
-    a = tg::StepArgs{};
-    a.npad = np;
-    a.slots = std::max(P.max_slots, 1);
-    a.ecap = std::max(P.max_entries, 1);
-    a.hcap = std::max(P.max_heavy, 1);
-    cudaError_t e = cudaSuccess;
-    s->smem = 0;
-    int64_t max_ne = 0, max_nact = 0, max_incw = 0, max_nh = 0, max_slots = 0, max_heavy = 0;
+// Per-tile launch records of a plan.
+std::vector<tg::TileInfo> tile_infos(const tg::Plan &P) {
     std::vector<tg::TileInfo> tiles(P.ntiles);
     for (int64_t t = 0; t < P.ntiles; t++) {
         tg::TileInfo &ti = tiles[t];
@@ -525,6 +507,89 @@ int build_device(titan_gb300_sim *s) {
         ti.inc_off = (int32_t)i0;
         ti.inc_words = (int32_t)(i1 - i0);
         ti.pad0 = ti.pad1 = ti.pad2 = 0;
+    }
+    return tiles;
+}
+
+// Stage layout of the warp-specialised kernel for these tiles (sized by
+// their largest): the offsets inside a stage, the halo-index and heavy-sum
+// capacities, and how many stages fit one SM's shared memory (nstages; the
+// kernel needs at least two).
+void ws_stage_layout(int prec, const std::vector<tg::TileInfo> &tiles, tg::WsLayout &W) {
+    auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
+    const int rec = tg::state_record_bytes(prec), ent = tg::entry_record_bytes(prec);
+    const int64_t rs = prec == P_FP64 ? 8 : 4;
+    int64_t mS = 0, mE = 0, mH = 0, mNh = 0, mA = 0, mI = 0;
+    for (const tg::TileInfo &ti : tiles) {
+        mS = std::max<int64_t>(mS, ti.nm + ti.nh);
+        mE = std::max<int64_t>(mE, ti.ne);
+        mH = std::max<int64_t>(mH, ti.nheavy);
+        mNh = std::max<int64_t>(mNh, ti.nh);
+        mA = std::max<int64_t>(mA, ti.nact);
+        mI = std::max<int64_t>(mI, ti.inc_words);
+    }
+    W.slots = (int32_t)al(mS * rec, 16);
+    W.act = (int32_t)al(W.slots + (mE + 1) * ent, 16);  // + the zero slot padding codes name
+    W.inc = (int32_t)al(W.act + mA * ent, 16);
+    W.stage = (int32_t)al(W.inc + mI * 2, 128);
+    W.idx_words = (int32_t)al(mNh, 4);
+    W.heavy_cap = (int32_t)std::max<int64_t>(1, mH);
+    const int64_t tail = 2 * (int64_t)W.idx_words * 4 + al(2 * 3 * (int64_t)W.heavy_cap * rs, 16) +
+                         tg::kWsMaxStages * (int64_t)sizeof(tg::TileInfo) + al((int64_t)sizeof(tg::DevParams), 16) +
+                         (2 * tg::kWsMaxStages + 2) * 8 + 32;
+    const int64_t room = 227 * 1024 - tail;
+    W.nstages = (int32_t)std::min<int64_t>(tg::kWsMaxStages, room / std::max<int64_t>(1, W.stage));
+}
+
+// Builds s->plan for a requested tile size (0: the default).  The default
+// tile of the warp-specialised form (208 masses) gives way to 192 when two
+// stages of the planned tiles would not fit one SM's shared memory.
+std::string plan_scene(titan_gb300_sim *s, int tile_masses, tg::PlanInput &in) {
+    in = plan_input(s, tile_masses);
+    std::string why = tg::build_plan(in, s->plan);
+    if (why.empty() && tile_masses == 0 && in.tile_cap == kWsDefaultTile) {
+        tg::WsLayout W{};
+        ws_stage_layout(s->prec, tile_infos(s->plan), W);
+        if (W.nstages < 2) {
+            in = plan_input(s, kWsFallbackTile);
+            why = tg::build_plan(in, s->plan);
+        }
+    }
+    s->plan_req = tile_masses;
+    return why;
+}
+
+// Builds the plan and all device buffers; positions/velocities come from the
+// host mirror.  Keeps T / steps.
+int build_device(titan_gb300_sim *s) {
+    s->free_device();
+    tg::PlanInput in;
+    const size_t rs = s->rsize();
+    if (s->plan_adopted && !s->started && s->plan_req == s->tile_masses) {
+        s->plan_adopted = false;  // the adopted plan serves this first start
+        in = plan_input(s, s->plan_tile);
+    } else {
+        s->plan_adopted = false;
+        std::string why = plan_scene(s, s->tile_masses, in);
+        if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+    }
+    s->plan_tile = in.tile_cap;
+    const tg::Plan &P = s->plan;
+    s->threads = s->threads_req > 0 ? s->threads_req : std::max(128, std::min(512, ((P.max_nm + 31) / 32) * 32));
+    s->npad = ((s->n + 127) / 128) * 128;
+    const int64_t np = s->npad;
+    auto &a = s->args;
+    a = tg::StepArgs{};
+    a.npad = np;
+    a.slots = std::max(P.max_slots, 1);
+    a.ecap = std::max(P.max_entries, 1);
+    a.hcap = std::max(P.max_heavy, 1);
+    cudaError_t e = cudaSuccess;
+    s->smem = 0;
+    int64_t max_ne = 0, max_nact = 0, max_incw = 0, max_nh = 0, max_slots = 0, max_heavy = 0;
+    std::vector<tg::TileInfo> tiles = tile_infos(P);
+    for (int64_t t = 0; t < P.ntiles; t++) {
+        const tg::TileInfo &ti = tiles[t];
         // ne + 1 force slots: the last holds the zero force padding codes name
         s->smem = std::max(s->smem, s->kernel_req == 3
                                         ? tg::tile_async_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy)
@@ -655,32 +720,8 @@ int build_device(titan_gb300_sim *s) {
     s->use_ws = false;
     const bool want_ws = s->kernel_req == 4 || (s->kernel_req == 0 && s->prec != P_FP64 && !tiles_run.empty());
     if (want_ws) {
-        auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
-        const int rec = tg::state_record_bytes(s->prec), ent = tg::entry_record_bytes(s->prec);
-        int64_t mS = 0, mE = 0, mH = 0;
-        for (const tg::TileInfo &ti : tiles_run) {
-            mS = std::max<int64_t>(mS, ti.nm + ti.nh);
-            mE = std::max<int64_t>(mE, ti.ne);
-            mH = std::max<int64_t>(mH, ti.nheavy);
-        }
-        int64_t mNh = 0, mA = 0, mI = 0;
-        for (const tg::TileInfo &ti : tiles_run) {
-            mNh = std::max<int64_t>(mNh, ti.nh);
-            mA = std::max<int64_t>(mA, ti.nact);
-            mI = std::max<int64_t>(mI, ti.inc_words);
-        }
         tg::WsLayout &W = a.ws;
-        W.slots = (int32_t)al(mS * rec, 16);
-        W.act = (int32_t)al(W.slots + (mE + 1) * ent, 16);  // + the zero slot padding codes name
-        W.inc = (int32_t)al(W.act + mA * ent, 16);
-        W.stage = (int32_t)al(W.inc + mI * 2, 128);
-        W.idx_words = (int32_t)al(mNh, 4);
-        W.heavy_cap = (int32_t)std::max<int64_t>(1, mH);
-        const int64_t tail = 2 * (int64_t)W.idx_words * 4 + al(2 * 3 * (int64_t)W.heavy_cap * (int64_t)rs, 16) +
-                             tg::kWsMaxStages * (int64_t)sizeof(tg::TileInfo) +
-                             al((int64_t)sizeof(tg::DevParams), 16) + (2 * tg::kWsMaxStages + 2) * 8 + 32;
-        const int64_t room = 227 * 1024 - tail;
-        W.nstages = (int32_t)std::min<int64_t>(tg::kWsMaxStages, room / std::max<int64_t>(1, W.stage));
+        ws_stage_layout(s->prec, tiles_run, W);
         if (W.nstages < 2 && s->kernel_req == 4)
             return s->fail(TITAN_GB300_ELIMIT, "two tiles do not fit in shared memory for the warp-specialised kernel");
     }
@@ -1056,6 +1097,7 @@ int titan_gb300_adopt_plan(titan_gb300_sim *s, const titan_gb300_sim *src) {
                        "actuated springs and bodies");
     s->plan = src->plan;
     s->plan_tile = src->plan_tile;
+    s->plan_req = src->plan_req;
     s->plan_adopted = true;
     return TITAN_GB300_OK;
 }
@@ -1064,8 +1106,8 @@ int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
     if (!s) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "plan_host is for scenes that have not started");
     if (s->n <= 0) return s->fail(TITAN_GB300_EINVAL, "no masses");
-    tg::PlanInput in = plan_input(s, tile_masses);
-    std::string why = tg::build_plan(in, s->plan);
+    tg::PlanInput in;
+    std::string why = plan_scene(s, tile_masses, in);
     if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
     s->plan_tile = in.tile_cap;
     s->plan_adopted = false;

