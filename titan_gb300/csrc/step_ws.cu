@@ -50,6 +50,14 @@ __host__ __device__ constexpr int ws_rec() { return PREC == P_FP32 ? 32 : 48; }
 __device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
+// Programmatic dependent launch (the step kernels of a graph run back to
+// back): launch_dependents lets the next grid start launching; wait blocks
+// until the preceding grid has completed and its writes are visible (no-op
+// when the launch has no programmatic predecessor).
+__device__ __forceinline__ void grid_dep_launch_dependents() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -105,8 +113,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
     DevParams *prm = reinterpret_cast<DevParams *>(smem + L.params);
     for (int q = threadIdx.x; q < (int)(sizeof(DevParams) / 16); q += blockDim.x)
         reinterpret_cast<int4 *>(prm)[q] = __ldg(reinterpret_cast<const int4 *>(a.prm) + q);
-    const StepTime tm = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + a.prm->launch_dt;
+    // the next step's grid may launch now: its CTAs take SMs as this grid's
+    // leave, and everything it does before its grid_dep_wait() reads only
+    // data no step writes (see the producer and the consumers below)
+    grid_dep_launch_dependents();
     const int ncw = (int)(blockDim.x >> 5) - 1;  // consumer warps (even)
     const int gw = ncw >> 1;                     // warps per group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -176,8 +186,11 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                 issue_chunks(st + L.act, reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * kSlot, ab,
                              &full[s]);
                 issue_chunks(st + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), ib, &full[s]);
-                issue_chunks(st, in + (int64_t)ti.mass_off * kRec, sb, &full[s]);
             }
+            // slab, actuation, incidence and halo-index blocks are constant
+            // across steps; the state records are the previous step's output
+            if (k == 0) grid_dep_wait();
+            if (lane == 0) issue_chunks(st, in + (int64_t)ti.mass_off * kRec, (uint32_t)ti.nm * kRec, &full[s]);
             // halo records, one per lane at a time (the producer issues for
             // every stage: its instruction count is on the critical path)
             const int32_t *ix = idxbuf + (k & 1) * L.idx_words;
@@ -197,6 +210,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
         }
     } else {
         // ---------------- consumer groups ----------------
+        grid_dep_wait();  // the time record is the previous step's output
+        const StepTime tm = step_time(a.tbuf[parity]);
+        if (threadIdx.x == 0 && blockIdx.x == 0) a.tbuf[parity ^ 1] = tm.T + a.prm->launch_dt;
         const int grp = warp / gw;
         const int gt = threadIdx.x - grp * gw * 32;  // thread index within the group
         const int gn = gw * 32;
@@ -340,9 +356,20 @@ cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas
     if (a.ntiles <= 0) return cudaSuccess;
     if (consumer_warps < 2 || consumer_warps > kWsMaxConsumerWarps || (consumer_warps & 1))
         return cudaErrorInvalidValue;
+    // programmatic stream serialisation: the next step's grid may start
+    // while this one drains (the kernel orders its dependent reads itself)
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3((consumer_warps + 1) * 32);
+    cfg.dynamicSmemBytes = (size_t)a.ws.total;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
-    return cudaLaunchKernel(ws_kernel(precision, integ), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
-                            (size_t)a.ws.total, s);
+    return cudaLaunchKernelExC(&cfg, ws_kernel(precision, integ), args);
 }
 
 }  // namespace tg
