@@ -195,11 +195,12 @@ int titan_gb300_kernel_info(const titan_gb300_sim *sim, int64_t out[4]);
  * persistent launch per step() call runs all nsteps steps of every bin with
  * the state held in shared memory; the remaining bodies take the per-step
  * kernels.  Results are bit-identical to the per-step kernels.
- *   mode -1 (default): automatic -- resident tiles (mode 2) when the
- *   kernel form is automatic (set_kernel 0), the integrator is symplectic
- *   Euler and every tile of the scene is halo-free (measured on GB300: 2.5x
+ *   mode -1 (default): automatic -- resident tiles (mode 2) for the
+ *   scene's halo-free tiles when the kernel form is automatic (set_kernel
+ *   0) and the integrator is symplectic Euler (measured on GB300: 2.5x
  *   faster than the per-step kernels on one 125-mass body, 2x on thousands
- *   of small bodies, equal in FP64), else off; 0 off; 1 bins of
+ *   of small bodies, 5 % on a batch whose small bodies alone are
+ *   halo-free), else off; 0 off; 1 bins of
  *   whole bodies, one thread per mass (bin_masses: bin capacity, rounded
  *   up to a multiple of 32; 0: the largest fitting body when at most 152
  *   bodies fit, else max(1024, largest fitting body); bodies above it are

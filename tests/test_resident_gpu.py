@@ -183,8 +183,9 @@ def test_resident_tiles_heavy_hub_bitwise():
 
 
 def test_automatic_resident_tiles_choice():
-    """By default resident tiles carry a scene whose tiles are all
-    halo-free (symplectic Euler, automatic kernel form), and nothing else."""
+    """By default resident tiles carry the halo-free tiles (symplectic
+    Euler, automatic kernel form): a whole small scene, the small bodies of
+    a batch beside the per-step kernels, nothing of a single large lattice."""
     small = wl.config1(contact=True)
     s = wl.make_sim(small, tg.FP32C)
     assert s.resident_info()["active"] == 2 and s.plan_info()["tiles"] == 1
@@ -196,6 +197,17 @@ def test_automatic_resident_tiles_choice():
     s = wl.make_sim(wl.config2(n_side=20), tg.FP32C)  # tiles with halos
     assert s.resident_info()["active"] == 0
     s.close()
+    mixed = batch(nbodies=24, seed=21, side_range=(3, 9), passive=False)  # 9^3 bodies span several tiles
+    s = wl.make_sim(mixed, tg.FP32C)
+    info = s.resident_info()
+    assert info["active"] == 2 and 0 < info["bins"] < s.plan_info()["tiles"]
+    assert s.kernel_info()["kernel"] == "warp-specialised"
+    s.step(1)
+    s.step(299)
+    a = s.get_state(acc=True, T=True)
+    s.close()
+    _, b = run(mixed, [1, 299], tg.FP32C, resident=(0, 0, 0))
+    assert_same(a, b)
     sc = dict(small, integrator=tg.VERLET)
     s = wl.make_sim(sc, tg.FP64)
     assert s.resident_info()["active"] == 0

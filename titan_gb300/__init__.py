@@ -324,8 +324,8 @@ class Sim:
 
     def set_resident(self, mode: int = 1, bin_masses: int = 0, threads: int = 0):
         """Resident launches (all steps of a call in one kernel): mode -1
-        automatic (the default: halo-free tiles when every tile is one and
-        the kernel form is automatic), 0 off, 1 bins of whole bodies (one
+        automatic (the default: the halo-free tiles, when the kernel form
+        is automatic), 0 off, 1 bins of whole bodies (one
         thread per mass), 2 halo-free tiles (the per-step kernels' two
         phases in shared memory); bin capacity in masses (mode 1) and CTA
         size (0: default)."""
