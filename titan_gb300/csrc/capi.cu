@@ -440,14 +440,40 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     in.type = s->type.empty() ? nullptr : s->type.data();
     in.nbodies = s->body_ptr.empty() ? 0 : (int64_t)s->body_ptr.size() - 1;
     in.body_ptr = s->body_ptr.empty() ? nullptr : s->body_ptr.data();
-    // default tile: 256 masses in FP64 (with two threads per mass: the FP64
-    // pipe wants the warps; 2.40 ms per 100^3 step against 2.50 with tiles
-    // of 128); in the FP32 forms 208 for the
-    // warp-specialised kernel (two stages fit one SM's shared memory; 192
-    // where they would not, plan_scene) and 256 for the per-tile forms
-    // (measured fastest on GB300, see profiles/)
+    // Default tile.  Large scenes: 256 masses in FP64 (with two threads per
+    // mass: the FP64 pipe wants the warps; 2.40 ms per 100^3 step against
+    // 2.50 with tiles of 128), 208 for the FP32 forms' warp-specialised
+    // kernel (two stages fit one SM's shared memory; 192 where they would
+    // not, plan_scene) and 256 for the per-tile forms.  Smaller scenes get
+    // smaller tiles so that their tiles cover the SMs: FP64 about 1.6 tiles
+    // per SM (tiles of 32 to 256 masses), the warp-specialised form about
+    // 4 (64 to 208); a body that fits the large-scene tile stays whole (a
+    // halo-free tile runs resident).  Measured on GB300, 20^3 lattice: FP64
+    // 37 us per step with 32-mass tiles against 90 with 256; FP32C 5.3 us
+    // with 64 against 6.5 with 208.
     const bool ws = s->kernel_req == 0 || s->kernel_req == 4;
-    in.tile_cap = tile_masses > 0 ? tile_masses : (s->prec == P_FP64 ? 256 : (ws ? kWsDefaultTile : 256));
+    if (tile_masses > 0) {
+        in.tile_cap = tile_masses;
+    } else {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            sms = 152;  // GB300
+        }
+        auto fit = [&](double per_sm, int lo, int hi) {
+            const int64_t t = (int64_t)((double)s->n / (per_sm * sms)) / 32 * 32;
+            return (int)std::max<int64_t>(lo, std::min<int64_t>(hi, t));
+        };
+        if (s->prec == P_FP64) {
+            in.tile_cap = fit(1.6, 32, 256);
+            in.whole_cap = 256;
+        } else if (ws) {
+            in.tile_cap = fit(4.0, 64, kWsDefaultTile);
+            in.whole_cap = kWsDefaultTile;
+        } else {
+            in.tile_cap = 256;
+        }
+    }
     in.heavy_threshold = 96;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)

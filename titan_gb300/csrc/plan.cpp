@@ -294,7 +294,8 @@ std::string build_plan(const PlanInput &in, Plan &P) {
             }
             code[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
         }
-        bisect(P.new2old.data() + b0, b1 - b0, in.tile_cap, qc, code, b0, leaf_end);
+        const int cap_b = (b1 - b0) <= (int64_t)in.whole_cap ? (int)(b1 - b0) : in.tile_cap;
+        bisect(P.new2old.data() + b0, b1 - b0, cap_b, qc, code, b0, leaf_end);
     }
     P.old2new.resize(n);
     for (int64_t i = 0; i < n; i++) P.old2new[P.new2old[i]] = (int32_t)i;

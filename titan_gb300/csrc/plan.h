@@ -26,6 +26,7 @@ struct PlanInput {
     int64_t nbodies = 0;                 // 0: one body
     const int64_t *body_ptr = nullptr;   // nbodies+1, creation-order ranges
     int tile_cap = 512;                  // masses per tile
+    int whole_cap = 0;                   // bodies of at most this many masses stay one tile (0: tile_cap)
     int slot_cap = 4095;                 // tile + halo slots per tile (12-bit)
     int entry_cap = 32767;               // slab entries per tile (15-bit)
     int heavy_threshold = 96;            // degree above this: warp-cooperative
