@@ -175,6 +175,69 @@ def test_plan_actuated_fixed_and_loops():
     validate(sc, plan_tables(sc, 64))
 
 
+def test_plan_tiles_are_compact_blocks():
+    """Recursive coordinate bisection: every tile of a 24^3 lattice is a
+    near-cubic block of lattice sites (no side more than twice another),
+    and the halos are those of blocks, not of runs of a space-filling
+    curve."""
+    n = 24
+    sc = wl.lattice_scene((0, 0, 1), (1, 1, 1), n, n, n)
+    P = plan_tables(sc, 192)
+    validate(sc, P)
+    tmo, new2old = P["tile_mass_off"], P["new2old"]
+    ijk = np.stack(np.unravel_index(np.arange(n ** 3), (n, n, n)), 1)  # lattice builder order: i, j, k
+    for t in range(tmo.size - 1):
+        c = ijk[new2old[tmo[t]:tmo[t + 1]]]
+        ext = c.max(0) - c.min(0) + 1
+        assert ext.max() <= 2 * ext.min(), (t, ext)
+        assert np.prod(ext) <= 2 * (tmo[t + 1] - tmo[t]), (t, ext)  # a block (cuts may split a layer)
+    assert P["tile_nh"].mean() < 1.6 * np.diff(tmo).mean()
+
+
+def test_plan_default_tile_adapts_and_keeps_small_bodies_whole():
+    """Default tiles: a small lattice gets tiles small enough to cover the
+    SMs; bodies that fit the large-scene tile (208 masses in FP32C) are one
+    tile each even then."""
+    small = wl.lattice_scene((0, 0, 1), (1, 1, 1), 20, 20, 20)
+    P = plan_tables(small, 0)
+    nm = np.diff(P["tile_mass_off"])
+    assert nm.max() <= 128 and P["tile_mass_off"].size - 1 >= 60
+    sc = wl.config3(nbodies=40, seed=3, side_range=(3, 7))
+    P = plan_tables(sc, 0)
+    bp = sc["body_ptr"]
+    sizes = np.diff(bp)
+    body_of_tile = P["body_of_tile"]
+    for b in range(sizes.size):
+        ntile = int(np.sum(body_of_tile == b))
+        if sizes[b] <= 208:
+            assert ntile == 1, (b, sizes[b], ntile)
+
+
+def bank_wavefronts(P, rec_mod=8):
+    """Mean 16-byte shared-memory wavefronts per quarter-warp endpoint load
+    in phase B (1.0 = conflict-free)."""
+    te, ends = P["tile_ent_off"], P["ent_ends"]
+    tot = cnt = 0
+    for t in range(te.size - 1):
+        a = (ends[te[t]:te[t + 1]] & 0xFFF).astype(np.int64)
+        b = ((ends[te[t]:te[t + 1]] >> 12) & 0xFFF).astype(np.int64)
+        for g0 in range(0, a.size, 8):
+            for arr in (a, b):
+                xs = np.unique(arr[g0:g0 + 8])
+                tot += np.bincount((3 * xs) % rec_mod, minlength=rec_mod).max()
+                cnt += 1
+    return tot / cnt
+
+
+def test_plan_slab_groups_avoid_bank_conflicts():
+    """The planner orders each tile's slab so that a quarter-warp's endpoint
+    records mostly fall in distinct bank groups (spring order alone gives
+    about 1.6-1.7 wavefronts per load on a lattice)."""
+    sc = wl.config2(n_side=16)
+    P = plan_tables(sc, 192)
+    assert bank_wavefronts(P) < 1.2
+
+
 def test_plan_heavy_hub():
     from tests.test_oracle import hub_scene
     sc = hub_scene(degree=300)
