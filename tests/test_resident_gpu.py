@@ -31,7 +31,9 @@ def batch(nbodies=40, seed=12, side_range=(3, 7), passive=True):
     return sc
 
 
-def run(sc, chunks, precision=tg.FP64, resident=(1, 0, 0), tile=0, edit=None):
+def run(sc, chunks, precision=tg.FP64, resident=(1, 0, 0), tile=128, edit=None):
+    # tile 128: every body of up to 128 masses is one tile in every precision
+    # (default FP64 tiles of small scenes are smaller, to spread over SMs)
     s = wl.make_sim(sc, precision, tile, resident=resident)
     for q, c in enumerate(chunks):
         s.step(c)
@@ -220,7 +222,7 @@ def test_set_integrator_leaves_resident_tiles_bitwise():
     sc = wl.actuate(wl.config1(contact=True), np.random.default_rng(8), 0.3, 0.1)
     out = []
     for res in ((2, 0, 0), (0, 0, 0)):
-        s = wl.make_sim(sc, tg.FP64, resident=res)
+        s = wl.make_sim(sc, tg.FP64, 128, resident=res)  # the body in one tile
         s.step(300)
         s.set_integrator(tg.RK2)
         s.step(200)

@@ -447,10 +447,13 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     // not, plan_scene) and 256 for the per-tile forms.  Smaller scenes get
     // smaller tiles so that their tiles cover the SMs: FP64 about 1.6 tiles
     // per SM (tiles of 32 to 256 masses), the warp-specialised form about
-    // 4 (64 to 208); a body that fits the large-scene tile stays whole (a
-    // halo-free tile runs resident).  Measured on GB300, 20^3 lattice: FP64
-    // 37 us per step with 32-mass tiles against 90 with 256; FP32C 5.3 us
-    // with 64 against 6.5 with 208.
+    // 4 (64 to 208).  In the FP32 forms a body that fits the large-scene
+    // tile stays whole (a halo-free tile runs resident: 2.0 us per step for
+    // the 5^3 lattice against 3.3 split in four); in FP64, bound by each
+    // SM's FP64 pipe, it is split like the rest (17.9 us in four tiles
+    // against 28.9 resident).  Measured on GB300, 20^3 lattice: FP64 37 us
+    // per step with 32-mass tiles against 90 with 256; FP32C 5.3 us with
+    // 64 against 6.5 with 208.
     const bool ws = s->kernel_req == 0 || s->kernel_req == 4;
     if (tile_masses > 0) {
         in.tile_cap = tile_masses;
@@ -465,8 +468,7 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
             return (int)std::max<int64_t>(lo, std::min<int64_t>(hi, t));
         };
         if (s->prec == P_FP64) {
-            in.tile_cap = fit(1.6, 32, 256);
-            in.whole_cap = 256;
+            in.tile_cap = fit(1.6, 32, 256);  // small bodies split too: FP64 binds per SM
         } else if (ws) {
             in.tile_cap = fit(4.0, 64, kWsDefaultTile);
             in.whole_cap = kWsDefaultTile;
