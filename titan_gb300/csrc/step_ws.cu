@@ -31,6 +31,7 @@
 #include "async_copy.cuh"
 #include "engine.h"
 #include "epilogue.cuh"
+#include "grid_dep.cuh"
 #include "state.cuh"
 #include "step_math.cuh"
 #include "tile_phases.cuh"
@@ -50,14 +51,6 @@ __host__ __device__ constexpr int ws_rec() { return PREC == P_FP32 ? 32 : 48; }
 __device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// Programmatic dependent launch (the step kernels of a graph run back to
-// back): launch_dependents lets the next grid start launching; wait blocks
-// until the preceding grid has completed and its writes are visible (no-op
-// when the launch has no programmatic predecessor).
-__device__ __forceinline__ void grid_dep_launch_dependents() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -358,18 +351,9 @@ cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas
         return cudaErrorInvalidValue;
     // programmatic stream serialisation: the next step's grid may start
     // while this one drains (the kernel orders its dependent reads itself)
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3((consumer_warps + 1) * 32);
-    cfg.dynamicSmemBytes = (size_t)a.ws.total;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
-    return cudaLaunchKernelExC(&cfg, ws_kernel(precision, integ), args);
+    return launch_programmatic(ws_kernel(precision, integ), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
+                               (size_t)a.ws.total, s);
 }
 
 }  // namespace tg
