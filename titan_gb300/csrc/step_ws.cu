@@ -40,7 +40,7 @@ namespace tg {
 
 namespace {
 
-constexpr int kBatchB = 2;  // slab entries per thread in flight (phase B)
+constexpr int kBatchB = 3;  // slab entries per thread in flight (phase B); 4 spills at the 128-register cap
 constexpr int kWsThreads = (kWsMaxConsumerWarps + 1) * 32;
 
 template <int PREC>
