@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <numeric>
@@ -96,12 +97,16 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
     };
     std::vector<int64_t> out;
     out.reserve(n);
+    std::vector<uint8_t> lr(n), rr(n);  // residues of the endpoint slots
+    for (int64_t q = 0; q < n; q++) {
+        lr[q] = (uint8_t)(ls[q] % (uint32_t)mod);
+        rr[q] = (uint8_t)(rs[q] % (uint32_t)mod);
+    }
     bool first = true;
     while ((int64_t)out.size() < n) {
         uint32_t lsl[8][2], rsl[8][2];
         int lcnt[8] = {0}, rcnt[8] = {0};
-        auto fits = [&](const uint32_t (*tab)[2], const int *cnt, uint32_t x) {
-            const int r = (int)(x % (uint32_t)mod);
+        auto fits = [&](const uint32_t (*tab)[2], const int *cnt, uint32_t x, int r) {
             for (int q = 0; q < cnt[r]; q++)
                 if (tab[r][q] == x) return true;
             return cnt[r] < cap;
@@ -125,7 +130,7 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
         for (int64_t q = head; q < n && taken < 8 && seen < kWindow;) {
             const int64_t nq = nx[q];
             seen++;
-            if (fits(lsl, lcnt, ls[q]) && fits(rsl, rcnt, rs[q])) {
+            if (fits(lsl, lcnt, ls[q], lr[q]) && fits(rsl, rcnt, rs[q], rr[q])) {
                 add(lsl, lcnt, ls[q]);
                 add(rsl, rcnt, rs[q]);
                 take(q);
@@ -152,9 +157,24 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
 // where they can.  Greedy per group: the entries with the most gather
 // references first, each to the free position whose residue the entry's
 // (quarter-warp, j) sets use least.
+// Scratch of gather_permute, reused from tile to tile: a spring -> slab
+// position table (open addressing; a slot is live when its stamp is the
+// current tile's) and the per-entry and per-set arrays.
+struct PermuteScratch {
+    std::vector<int64_t> hkey;
+    std::vector<int32_t> hval;
+    std::vector<uint32_t> hstamp;
+    uint32_t stamp = 0;
+    std::vector<int64_t> seq, out;
+    std::vector<int32_t> k0, k1;
+    std::vector<uint8_t> cnt;
+};
+
 void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64_t lo, int64_t hi,
-                    const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold) {
-    std::vector<int64_t> seq(act);
+                    const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold,
+                    PermuteScratch &W) {
+    std::vector<int64_t> &seq = W.seq;
+    seq.assign(act.begin(), act.end());
     seq.insert(seq.end(), rest.begin(), rest.end());
     const int64_t ne = (int64_t)seq.size(), na = (int64_t)act.size(), nm = hi - lo;
     if (ne <= 1) return;
@@ -162,19 +182,25 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
     // (the global spring-indexed array would be read at scattered places)
     int64_t hcap = 16;
     while (hcap < 2 * ne) hcap <<= 1;
-    std::vector<int64_t> hkey((size_t)hcap, -1);
-    std::vector<int32_t> hval((size_t)hcap, 0);
+    if ((int64_t)W.hkey.size() < hcap) {
+        W.hkey.assign((size_t)hcap, -1);
+        W.hval.assign((size_t)hcap, 0);
+        W.hstamp.assign((size_t)hcap, 0);
+        W.stamp = 0;
+    }
+    const uint32_t stamp = ++W.stamp;
     auto hslot = [&](int64_t sp) {
         uint64_t h = ((uint64_t)sp * 0x9E3779B97F4A7C15ULL) >> 20;
         for (;; h++) {
             const size_t q = (size_t)(h & (uint64_t)(hcap - 1));
-            if (hkey[q] == sp || hkey[q] < 0) return q;
+            if (W.hstamp[q] != stamp || W.hkey[q] == sp) return q;
         }
     };
     for (int64_t p = 0; p < ne; p++) {
         const size_t q = hslot(seq[p]);
-        hkey[q] = seq[p];
-        hval[q] = (int32_t)p;
+        W.hkey[q] = seq[p];
+        W.hval[q] = (int32_t)p;
+        W.hstamp[q] = stamp;
     }
     int64_t maxd = 1;
     for (int64_t m = lo; m < hi; m++) {
@@ -182,18 +208,22 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
         if (d <= heavy_threshold) maxd = std::max(maxd, d);
     }
     // the (quarter-warp, incidence position) sets each entry belongs to
-    std::vector<int32_t> k0(ne, -1), k1(ne, -1);
+    std::vector<int32_t> &k0 = W.k0, &k1 = W.k1;
+    k0.assign((size_t)ne, -1);
+    k1.assign((size_t)ne, -1);
     for (int64_t m = lo; m < hi; m++) {
         const int64_t d = ip[m + 1] - ip[m];
         if (d > heavy_threshold) continue;
         for (int64_t j = 0; j < d; j++) {
-            const int64_t p = hval[hslot(isp[ip[m] + j])];
+            const int64_t p = W.hval[hslot(isp[ip[m] + j])];
             const int32_t key = (int32_t)(((m - lo) >> 3) * maxd + j);
             (k0[p] < 0 ? k0[p] : k1[p]) = key;
         }
     }
-    std::vector<uint8_t> cnt((size_t)(((nm + 7) >> 3) * maxd * 8), 0);
-    std::vector<int64_t> out(seq);
+    std::vector<uint8_t> &cnt = W.cnt;
+    cnt.assign((size_t)(((nm + 7) >> 3) * maxd * 8), 0);
+    std::vector<int64_t> &out = W.out;
+    out.assign(seq.begin(), seq.end());
     for (int64_t b0 = 0; b0 < ne; b0 += 8) {
         const int64_t b1 = std::min<int64_t>(b0 + 8, ne);
         for (int side = 0; side < 2; side++) {
@@ -209,12 +239,16 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
             bool taken[8] = {false};
             for (int q = 0; q < n8; q++) {
                 const int64_t x = ord[q];
+                // the entry's use of each residue, summed over its two sets
+                // (eight byte counters added at once: each is at most 8)
+                uint64_t c0 = 0, c1 = 0;
+                if (k0[x] >= 0) std::memcpy(&c0, &cnt[(size_t)k0[x] * 8], 8);
+                if (k1[x] >= 0) std::memcpy(&c1, &cnt[(size_t)k1[x] * 8], 8);
+                const uint64_t cs = c0 + c1;
                 int best = -1, bestc = 1 << 30;
                 for (int64_t p = s0; p < s1; p++) {
                     if (taken[p - s0]) continue;
-                    const int r = (int)(p & 7);
-                    const int c = (k0[x] >= 0 ? cnt[(size_t)k0[x] * 8 + r] : 0) +
-                                  (k1[x] >= 0 ? cnt[(size_t)k1[x] * 8 + r] : 0);
+                    const int c = (int)((cs >> (8 * (p & 7))) & 0xff);
                     if (c < bestc) bestc = c, best = (int)(p - s0);
                 }
                 taken[best] = true;
@@ -348,6 +382,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     P.deg.assign(n, 0);
 
     size_t leaf = 0;
+    PermuteScratch perm_scratch;
     for (int64_t b = 0; b < P.nbodies; b++) {
         std::deque<std::pair<int64_t, int64_t>> work;
         for (; leaf < leaf_end.size() && leaf_end[leaf] <= bptr[b + 1]; leaf++)
@@ -429,7 +464,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                     lead = tail;
                 }
             }
-            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold);
+            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold, perm_scratch);
             int32_t e = 0;
             for (auto *v : {&ents_act, &ents})
                 for (int64_t s : *v) {
