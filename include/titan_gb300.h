@@ -147,7 +147,12 @@ int titan_gb300_set_body_plane(titan_gb300_sim *sim, int64_t body, const double 
 /* Replaces start() (src/sim.cu:1349-1390) minus the thread spawn: builds the
  * tile plan (spatial renumbering, spring slabs, per-mass incidence), uploads
  * the structure-of-arrays state and resets time to 0.  tile_masses = 0 picks
- * the tuned default. */
+ * the tuned default: near-cubic tiles of up to 208 masses for the FP32 forms'
+ * warp-specialised kernel (192 where two of them would not fit one SM's
+ * shared memory), 256 for the per-tile forms and in FP64; smaller for small
+ * scenes, so that their tiles cover the SMs (about 4 tiles per SM, at least
+ * 64 masses, in the FP32 forms; about 1.6, at least 32, in FP64); in the
+ * FP32 forms a body that fits the large tile stays one tile. */
 int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
 
 /* Takes src's tile plan for this handle's next start() instead of building
@@ -155,7 +160,8 @@ int titan_gb300_start(titan_gb300_sim *sim, int tile_masses);
  * src must have been planned (plan_host) or started; both handles must have
  * the same precision, kernel form, masses, springs (ends), fixed masses,
  * actuated springs and bodies -- positions, parameters and constraints may
- * differ.  The plan is used when start()'s tile size equals src's.  Results
+ * differ.  The plan is used when start()'s requested tile size equals the
+ * one src was planned with (0 for both: the default).  Results
  * do not depend on which plan a scene runs with. */
 int titan_gb300_adopt_plan(titan_gb300_sim *sim, const titan_gb300_sim *src);
 
