@@ -213,6 +213,46 @@ def test_plan_default_tile_adapts_and_keeps_small_bodies_whole():
             assert ntile == 1, (b, sizes[b], ntile)
 
 
+def denser_lattice(n, extra=1, seed=1):
+    """A lattice plus `extra` springs per mass to random masses within three
+    lattice steps (larger slabs and halos per tile than a plain lattice)."""
+    sc = wl.lattice_scene((0, 0, 1), (1, 1, 1), n, n, n)
+    pos = sc["pos"]
+    N = pos.shape[0]
+    rng = np.random.default_rng(seed)
+    idx = np.arange(N)
+    ijk = np.stack(np.unravel_index(idx, (n, n, n)), 1)
+    L, R = [], []
+    for _ in range(extra):
+        tgt = np.clip(ijk + rng.integers(-3, 4, size=(N, 3)), 0, n - 1)
+        j = np.ravel_multi_index(tgt.T, (n, n, n))
+        keep = j != idx
+        L.append(idx[keep])
+        R.append(j[keep])
+    L = np.concatenate(L).astype(np.int32)
+    R = np.concatenate(R).astype(np.int32)
+    for key, val in (("k", 1e3), ("damping", 0.0), ("omega", 0.0), ("amp", 0.2), ("phase", 0.0)):
+        sc[key] = np.concatenate([sc[key], np.full(L.size, val)])
+    sc["rest"] = np.concatenate([sc["rest"], np.linalg.norm(pos[L] - pos[R], axis=1)])
+    sc["type"] = np.concatenate([sc["type"], np.zeros(L.size, np.int32)])
+    sc["left"] = np.concatenate([sc["left"], L])
+    sc["right"] = np.concatenate([sc["right"], R])
+    return sc
+
+
+def test_plan_default_tile_falls_back_when_two_stages_do_not_fit():
+    """Large scenes plan 208-mass tiles for the warp-specialised kernel, or
+    192 when two stages of the 208-mass tiles would not fit one SM's shared
+    memory (checked on the host from the plan itself)."""
+    plain = wl.lattice_scene((0, 0, 1), (1, 1, 1), 52, 52, 52)
+    d, p208 = plan_tables(plain, 0), plan_tables(plain, 208)
+    assert all(np.array_equal(d[k], p208[k]) for k in d)
+    dense = denser_lattice(52)
+    d, p192, p208 = plan_tables(dense, 0), plan_tables(dense, 192), plan_tables(dense, 208)
+    assert all(np.array_equal(d[k], p192[k]) for k in d)
+    assert p208["tile_mass_off"].size < p192["tile_mass_off"].size
+
+
 def bank_wavefronts(P, rec_mod=8):
     """Mean 16-byte shared-memory wavefronts per quarter-warp endpoint load
     in phase B (1.0 = conflict-free)."""
