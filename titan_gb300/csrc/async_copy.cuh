@@ -47,6 +47,33 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// An L2 cache policy for data read once per step (evict first), for the
+// bulk copies below: the slab, actuation and incidence blocks then leave L2
+// before the state records, which halo gathers and the next step re-read.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+// 1-D bulk copy with an L2 cache-policy hint (same rules as bulk_g2s)
+__device__ __forceinline__ void bulk_g2s_hint(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
+                                              uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(smem_u32(dst)),
+        "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+__device__ __forceinline__ uint32_t issue_chunks_hint(uint8_t *dst, const uint8_t *src, uint32_t bytes, uint64_t *bar,
+                                                      uint64_t pol) {
+    constexpr uint32_t kChunk = 32768;
+    for (uint32_t o = 0; o < bytes; o += kChunk) {
+        uint32_t b = bytes - o < kChunk ? bytes - o : kChunk;
+        bulk_g2s_hint(dst + o, src + o, b, bar, pol);
+    }
+    return bytes;
+}
+
 // Bulk copy in pieces of at most 32 KB (each 16-byte aligned, a multiple of
 // 16 bytes when the total is); returns the byte count.
 __device__ __forceinline__ uint32_t issue_chunks(uint8_t *dst, const uint8_t *src, uint32_t bytes, uint64_t *bar) {

@@ -174,11 +174,14 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                 const uint32_t eb = (uint32_t)ti.ne * kSlot, ab = (uint32_t)ti.nact * kSlot;
                 const uint32_t ib = (uint32_t)ti.inc_words * 2u, sb = (uint32_t)ti.nm * kRec;
                 mbar_expect_tx(&full[s], eb + ab + ib + sb);
-                issue_chunks(st + L.slots, reinterpret_cast<const uint8_t *>(a.ent) + (int64_t)ti.ent_off * kSlot,
-                             eb, &full[s]);
-                issue_chunks(st + L.act, reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * kSlot, ab,
-                             &full[s]);
-                issue_chunks(st + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), ib, &full[s]);
+                // read once per step: evict first from L2
+                const uint64_t pol = l2_evict_first_policy();
+                issue_chunks_hint(st + L.slots,
+                                  reinterpret_cast<const uint8_t *>(a.ent) + (int64_t)ti.ent_off * kSlot, eb, &full[s],
+                                  pol);
+                issue_chunks_hint(st + L.act, reinterpret_cast<const uint8_t *>(a.act) + (int64_t)ti.ent_off * kSlot,
+                                  ab, &full[s], pol);
+                issue_chunks_hint(st + L.inc, reinterpret_cast<const uint8_t *>(a.inc + ti.inc_off), ib, &full[s], pol);
             }
             // slab, actuation, incidence and halo-index blocks are constant
             // across steps; the state records are the previous step's output
