@@ -2,6 +2,8 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <thread>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <deque>
@@ -157,17 +159,44 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
 // where they can.  Greedy per group: the entries with the most gather
 // references first, each to the free position whose residue the entry's
 // (quarter-warp, j) sets use least.
-// Scratch of gather_permute, reused from tile to tile: a spring -> slab
+// Scratch of the slab ordering, reused from tile to tile: a spring -> slab
 // position table (open addressing; a slot is live when its stamp is the
-// current tile's) and the per-entry and per-set arrays.
+// current round's) and the per-entry and per-set arrays of gather_permute.
 struct PermuteScratch {
     std::vector<int64_t> hkey;
     std::vector<int32_t> hval;
     std::vector<uint32_t> hstamp;
     uint32_t stamp = 0;
+    int64_t hcap = 0;
     std::vector<int64_t> seq, out;
     std::vector<int32_t> k0, k1;
     std::vector<uint8_t> cnt;
+
+    void begin(int64_t ne) {  // an empty table for up to ne springs
+        int64_t c = 16;
+        while (c < 2 * ne) c <<= 1;
+        if ((int64_t)hkey.size() < c) {
+            hkey.assign((size_t)c, -1);
+            hval.assign((size_t)c, 0);
+            hstamp.assign((size_t)c, 0);
+            stamp = 0;
+        }
+        hcap = c;
+        ++stamp;
+    }
+    size_t probe(int64_t sp) const {
+        for (uint64_t h = ((uint64_t)sp * 0x9E3779B97F4A7C15ULL) >> 20;; h++) {
+            const size_t q = (size_t)(h & (uint64_t)(hcap - 1));
+            if (hstamp[q] != stamp || hkey[q] == sp) return q;
+        }
+    }
+    void put(int64_t sp, int32_t v) {
+        const size_t q = probe(sp);
+        hkey[q] = sp;
+        hval[q] = v;
+        hstamp[q] = stamp;
+    }
+    int32_t get(int64_t sp) const { return hval[probe(sp)]; }
 };
 
 void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64_t lo, int64_t hi,
@@ -179,29 +208,9 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
     const int64_t ne = (int64_t)seq.size(), na = (int64_t)act.size(), nm = hi - lo;
     if (ne <= 1) return;
     // spring -> position of this tile, in a small open-addressing table
-    // (the global spring-indexed array would be read at scattered places)
-    int64_t hcap = 16;
-    while (hcap < 2 * ne) hcap <<= 1;
-    if ((int64_t)W.hkey.size() < hcap) {
-        W.hkey.assign((size_t)hcap, -1);
-        W.hval.assign((size_t)hcap, 0);
-        W.hstamp.assign((size_t)hcap, 0);
-        W.stamp = 0;
-    }
-    const uint32_t stamp = ++W.stamp;
-    auto hslot = [&](int64_t sp) {
-        uint64_t h = ((uint64_t)sp * 0x9E3779B97F4A7C15ULL) >> 20;
-        for (;; h++) {
-            const size_t q = (size_t)(h & (uint64_t)(hcap - 1));
-            if (W.hstamp[q] != stamp || W.hkey[q] == sp) return q;
-        }
-    };
-    for (int64_t p = 0; p < ne; p++) {
-        const size_t q = hslot(seq[p]);
-        W.hkey[q] = seq[p];
-        W.hval[q] = (int32_t)p;
-        W.hstamp[q] = stamp;
-    }
+    // (a global spring-indexed array would be read at scattered places)
+    W.begin(ne);
+    for (int64_t p = 0; p < ne; p++) W.put(seq[p], (int32_t)p);
     int64_t maxd = 1;
     for (int64_t m = lo; m < hi; m++) {
         const int64_t d = ip[m + 1] - ip[m];
@@ -215,7 +224,7 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
         const int64_t d = ip[m + 1] - ip[m];
         if (d > heavy_threshold) continue;
         for (int64_t j = 0; j < d; j++) {
-            const int64_t p = W.hval[hslot(isp[ip[m] + j])];
+            const int64_t p = W.get(isp[ip[m] + j]);
             const int32_t key = (int32_t)(((m - lo) >> 3) * maxd + j);
             (k0[p] < 0 ? k0[p] : k1[p]) = key;
         }
@@ -262,6 +271,77 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
     act.assign(out.begin(), out.begin() + na);
     rest.assign(out.begin() + na, out.end());
 }
+
+// Final slab order of tile t (bank_order on each part, then
+// gather_permute), its entry words, and the incidence codes of its masses
+// (ELL block and heavy lists), written into the tile's own ranges of P's
+// tables, which the sequential pass laid out (entries in spring order, code
+// slots, heavy lists).
+void order_tile(const PlanInput &in, Plan &P, int64_t t, const std::vector<int32_t> &L,
+                const std::vector<int32_t> &R, const std::vector<int64_t> &ip, const std::vector<int64_t> &isp,
+                const std::vector<int8_t> &isg, PermuteScratch &W) {
+    const int64_t lo = P.tile_mass_off[t], hi = P.tile_mass_off[t + 1], nm = hi - lo;
+    const int64_t e0 = P.tile_ent_off[t], e1 = P.tile_ent_off[t + 1], na = P.tile_nact[t];
+    const int32_t *halo = P.halo.data() + P.tile_halo_off[t];
+    const int64_t nh = P.tile_nh[t];
+    auto slot = [&](int32_t x) -> uint32_t {  // tile masses, then the sorted halo
+        if (x >= lo && x < hi) return (uint32_t)(x - lo);
+        return (uint32_t)(nm + (std::lower_bound(halo, halo + nh, x) - halo));
+    };
+    std::vector<int64_t> ents_act(P.ent_spring.begin() + e0, P.ent_spring.begin() + e0 + na);
+    std::vector<int64_t> ents(P.ent_spring.begin() + e0 + na, P.ent_spring.begin() + e1);
+    {
+        // the non-actuated part continues the actuated part's last group
+        uint32_t lead_ls[8], lead_rs[8];
+        int lead = 0;
+        for (auto *v : {&ents_act, &ents}) {
+            std::vector<uint32_t> ls(v->size()), rs(v->size());
+            for (size_t q = 0; q < v->size(); q++) {
+                ls[q] = slot(L[(*v)[q]]);
+                rs[q] = slot(R[(*v)[q]]);
+            }
+            bank_order(*v, ls, rs, in.slot_bytes, lead_ls, lead_rs, lead);
+            // the open group after this part: its last (lead + size) % 8
+            // entries of the carried ones followed by this part's
+            std::vector<uint32_t> cl(lead_ls, lead_ls + lead), cr(lead_rs, lead_rs + lead);
+            for (int64_t sp : *v) {
+                cl.push_back(slot(L[sp]));
+                cr.push_back(slot(R[sp]));
+            }
+            const int tail = (int)(cl.size() % 8);
+            std::copy(cl.end() - tail, cl.end(), lead_ls);
+            std::copy(cr.end() - tail, cr.end(), lead_rs);
+            lead = tail;
+        }
+    }
+    gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold, W);
+    W.begin(e1 - e0);
+    int64_t e = e0;
+    for (auto *v : {&ents_act, &ents})
+        for (int64_t sp : *v) {
+            W.put(sp, (int32_t)(e - e0));
+            P.ent_spring[e] = sp;
+            P.ent_ends[e] = pack_ends(slot(L[sp]), slot(R[sp]), in.type ? (uint32_t)in.type[sp] : 0u);
+            e++;
+        }
+    auto code_of = [&](int64_t q) -> uint16_t { return (uint16_t)(W.get(isp[q]) | (isg[q] < 0 ? 0x8000 : 0)); };
+    int64_t hv = P.tile_heavy_off[t];
+    for (int64_t w = P.tile_warp_off[t]; w < P.tile_warp_off[t + 1]; w++) {
+        const int64_t m0 = lo + 32 * (w - P.tile_warp_off[t]), m1 = std::min(m0 + 32, hi);
+        const uint32_t off = P.warp_inc_off[w];
+        for (int64_t m = m0; m < m1; m++) {
+            const int64_t d = ip[m + 1] - ip[m];
+            if (d <= in.heavy_threshold) {
+                for (int64_t j = 0; j < d; j++)
+                    P.inc[ell_index(off, (uint32_t)(m - m0), (uint32_t)j)] = code_of(ip[m] + j);
+            } else {
+                const uint32_t h0 = P.heavy_inc_off[hv++];
+                for (int64_t q = ip[m]; q < ip[m + 1]; q++) P.heavy_inc[h0 + (q - ip[m])] = code_of(q);
+            }
+        }
+    }
+}
+
 
 }  // namespace
 
@@ -367,9 +447,7 @@ std::string build_plan(const PlanInput &in, Plan &P) {
 
     // ---- tiles ------------------------------------------------------------
     std::vector<int64_t> smark(ns, -1);
-    std::vector<int32_t> elocal(ns, 0);
     std::vector<int64_t> hmark(n, -1);
-    std::vector<int32_t> hslot(n, 0);
     std::vector<int64_t> ents, ents_act;
     std::vector<int32_t> halo;
     int64_t attempt = 0;
@@ -382,7 +460,6 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     P.deg.assign(n, 0);
 
     size_t leaf = 0;
-    PermuteScratch perm_scratch;
     for (int64_t b = 0; b < P.nbodies; b++) {
         std::deque<std::pair<int64_t, int64_t>> work;
         for (; leaf < leaf_end.size() && leaf_end[leaf] <= bptr[b + 1]; leaf++)
@@ -430,48 +507,14 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 work.emplace_front(lo, mid);
                 continue;
             }
-            // commit tile (slab: actuated entries first, each part in spring
-            // order, then grouped for conflict-free endpoint loads)
+            // commit the tile's layout; its slab order, entry words and
+            // incidence codes are filled in by order_tile() below
             std::sort(ents_act.begin(), ents_act.end());
             std::sort(ents.begin(), ents.end());
             std::sort(halo.begin(), halo.end());
             const int64_t nh = (int64_t)halo.size();
-            for (int64_t i = 0; i < nh; i++) hslot[halo[i]] = (int32_t)(nm + i);
-            auto slot = [&](int32_t x) -> uint32_t {
-                return (x >= lo && x < hi) ? (uint32_t)(x - lo) : (uint32_t)hslot[x];
-            };
-            {
-                // the non-actuated part continues the actuated part's last group
-                uint32_t lead_ls[8], lead_rs[8];
-                int lead = 0;
-                for (auto *v : {&ents_act, &ents}) {
-                    std::vector<uint32_t> ls(v->size()), rs(v->size());
-                    for (size_t q = 0; q < v->size(); q++) {
-                        ls[q] = slot(L[(*v)[q]]);
-                        rs[q] = slot(R[(*v)[q]]);
-                    }
-                    bank_order(*v, ls, rs, in.slot_bytes, lead_ls, lead_rs, lead);
-                    // the open group after this part: its last (lead + size) % 8
-                    // entries of the carried ones followed by this part's
-                    std::vector<uint32_t> cl(lead_ls, lead_ls + lead), cr(lead_rs, lead_rs + lead);
-                    for (int64_t sp : *v) {
-                        cl.push_back(slot(L[sp]));
-                        cr.push_back(slot(R[sp]));
-                    }
-                    const int tail = (int)(cl.size() % 8);
-                    std::copy(cl.end() - tail, cl.end(), lead_ls);
-                    std::copy(cr.end() - tail, cr.end(), lead_rs);
-                    lead = tail;
-                }
-            }
-            gather_permute(ents_act, ents, lo, hi, ip, isp, in.heavy_threshold, perm_scratch);
-            int32_t e = 0;
-            for (auto *v : {&ents_act, &ents})
-                for (int64_t s : *v) {
-                    elocal[s] = e++;
-                    P.ent_ends.push_back(pack_ends(slot(L[s]), slot(R[s]), in.type ? (uint32_t)in.type[s] : 0u));
-                    P.ent_spring.push_back(s);
-                }
+            for (auto *v : {&ents_act, &ents}) P.ent_spring.insert(P.ent_spring.end(), v->begin(), v->end());
+            P.ent_ends.resize(P.ent_spring.size(), 0u);
             P.halo.insert(P.halo.end(), halo.begin(), halo.end());
             while (P.halo.size() % 4) P.halo.push_back(halo.empty() ? (int32_t)lo : halo.back());
             P.tile_nh.push_back((int32_t)nh);
@@ -489,26 +532,19 @@ std::string build_plan(const PlanInput &in, Plan &P) {
                 width = (width + 3) & ~int64_t(3);
                 if (P.inc.size() > 0xffffffffULL - (uint64_t)(width * 32))
                     return "incidence table exceeds 2^32 words";
-                uint32_t off = (uint32_t)P.inc.size();
-                P.warp_inc_off.push_back(off);
+                P.warp_inc_off.push_back((uint32_t)P.inc.size());
                 // padding codes name slot ne, one past the tile's entries: a
                 // kernel that keeps a zero force there can sum whole words
                 P.inc.resize(P.inc.size() + (size_t)(width * 32), (uint16_t)ne);
                 for (int64_t m = m0; m < m1; m++) {
                     int64_t d = ip[m + 1] - ip[m];
-                    int64_t lane = m - m0;
-                    auto code_of = [&](int64_t q) -> uint16_t {
-                        return (uint16_t)(elocal[isp[q]] | (isg[q] < 0 ? 0x8000 : 0));
-                    };
                     if (d <= in.heavy_threshold) {
                         P.deg[m] = (uint8_t)d;
-                        for (int64_t j = 0; j < d; j++)
-                            P.inc[ell_index(off, (uint32_t)lane, (uint32_t)j)] = code_of(ip[m] + j);
                     } else {
                         P.deg[m] = 255;
                         P.heavy_local.push_back((uint16_t)(m - lo));
                         P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
-                        for (int64_t q = ip[m]; q < ip[m + 1]; q++) P.heavy_inc.push_back(code_of(q));
+                        P.heavy_inc.resize(P.heavy_inc.size() + (size_t)d, 0);
                         nheavy++;
                     }
                 }
@@ -527,6 +563,23 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     }
     P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
     P.ntiles = (int64_t)P.body_of_tile.size();
+
+    // ---- slab order, entry words and incidence codes, tiles in parallel ---
+    // (each tile writes only its own ranges of the tables)
+    {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int nt = (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), std::max<int64_t>(1, P.ntiles / 8));
+        std::atomic<int64_t> next{0};
+        auto worker = [&]() {
+            PermuteScratch scratch;
+            for (int64_t t; (t = next.fetch_add(1)) < P.ntiles;)
+                order_tile(in, P, t, L, R, ip, isp, isg, scratch);
+        };
+        std::vector<std::thread> pool;
+        for (int q = 1; q < nt; q++) pool.emplace_back(worker);
+        worker();
+        for (auto &th : pool) th.join();
+    }
     return "";
 }
 
