@@ -278,6 +278,17 @@ def test_plan_slab_groups_avoid_bank_conflicts():
     assert bank_wavefronts(P) < 1.2
 
 
+def test_plan_is_deterministic():
+    """The planner orders tile slabs on several host threads; two plans of
+    the same scene are the same, table for table."""
+    sc = wl.config3(nbodies=48, seed=11, side_range=(3, 9))
+    wl.actuate(sc, np.random.default_rng(4), 0.3, 0.1)
+    a, b = plan_tables(sc, 0), plan_tables(sc, 0)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    validate(sc, a)
+
+
 def test_plan_heavy_hub():
     from tests.test_oracle import hub_scene
     sc = hub_scene(degree=300)
