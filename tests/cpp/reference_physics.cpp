@@ -315,8 +315,60 @@ static void stl_import_test() {
     sim.stop();
 }
 
+// Throws std::runtime_error whose message contains `what`.
+template <class F>
+static bool throws_with(F &&f, const char *what) {
+    try {
+        f();
+    } catch (const std::runtime_error &e) {
+        return std::strstr(e.what(), what) != nullptr;
+    }
+    return false;
+}
+
+// The reference's misuse conventions before start() (src/sim.cu:798-806,
+// 1348-1356, 1484-1495, 590, 944): start() without masses, a non-positive
+// time step and resume() before start() throw with the reference's messages;
+// get() before start() prints and leaves the host objects alone.  Host-only
+// bulk edits (src/sim.cu:780-796) apply before start.  No device is touched.
+static void errors_test() {
+    titan::Simulation sim;
+    EXPECT_TRUE(throws_with([&] { sim.start(); }, "No masses have been added"));
+    EXPECT_TRUE(throws_with([&] { sim.setTimeStep(0.0); }, "Cannot set time step to negative or zero value."));
+    EXPECT_TRUE(throws_with([&] { sim.setTimeStep(-1e-4); }, "Cannot set time step to negative or zero value."));
+    EXPECT_NEAR(sim.getTimeStep(), 0.0001, 0);
+    sim.setTimeStep(2e-4);
+    EXPECT_NEAR(sim.getTimeStep(), 2e-4, 0);
+    EXPECT_TRUE(throws_with([&] { sim.resume(); }, "You cannot resume a simulation before calling sim.start()"));
+    EXPECT_TRUE(throws_with([&] { sim.setPrecision(3); }, "precision must be"));
+
+    titan::Mass *a = sim.createMass(Vec(0, 0, 1));
+    titan::Mass *b = sim.createMass(Vec(0, 0, 2));
+    titan::Spring *s = sim.createSpring(a, b);
+    EXPECT_TRUE(sim.masses.size() == 2 && sim.springs.size() == 1);
+    EXPECT_NEAR(s->_rest, 1.0, 1e-15);
+    sim.setAllMassValues(0.5);  // adds, as the reference does
+    EXPECT_NEAR(a->m, 0.6, 1e-15);
+    sim.setAllSpringConstantValues(123.0);
+    EXPECT_NEAR(s->_k, 123.0, 0);
+    b->pos = Vec(0, 0, 4);
+    sim.defaultRestLengths();
+    EXPECT_NEAR(s->_rest, 3.0, 1e-15);
+
+    a->pos = Vec(7, 8, 9);
+    sim.get(a);  // not started: prints, changes nothing
+    EXPECT_NEAR(a->pos[0], 7, 0);
+    titan::Container *c = sim.createContainer();
+    c->add(a);
+    sim.get(c);
+    EXPECT_NEAR(a->pos[2], 9, 0);
+    EXPECT_TRUE(throws_with([&] { sim.resume(); }, "You cannot resume"));
+    sim.setBreakpoint(1.0);  // allowed before start
+}
+
 int main(int argc, char **argv) {
     std::map<std::string, void (*)()> tests = {
+        {"errors_test", errors_test},
         {"simple_test", simple_test},         {"energy_test", energy_test},
         {"external_test", external_test},     {"external_acc_test", external_acc_test},
         {"multiagent_test", multiagent_test}, {"rotate_test", rotate_test},
