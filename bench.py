@@ -3,7 +3,7 @@
 
 Workload: the single large lattice -- 100^3 = 1,000,000 masses and
 12,731,796 springs (k log-uniform [1e3, 1e5], damping 0.1, 20% actuated),
-frictional plane and a fixed ball, dt = 1e-4 (titan_gb300.workloads.config2).
+frictional plane and a fixed ball, dt = 1e-4 (titan_gb300.workloads.actuated_lattice).
 A step is one time step of the whole lattice; its working set (~0.4-0.6 GB)
 is larger than L2, so no flush is needed between steps.
 
@@ -221,7 +221,7 @@ def run_ours(a, rank, world, local):
 
 
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
-    sc = wl.config2(a.side)
+    sc = wl.actuated_lattice(a.side)
     ns, nm = sc["left"].size, sc["pos"].shape[0]
     peak, peak_kind = peaks()
 
@@ -305,7 +305,7 @@ def run_ours(a, rank, world, local):
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": a.precision, "data": "synthetic (seeded lattice, BASELINE single-lattice configuration)",
+        "dtype": a.precision, "data": "synthetic (seeded actuated lattice on a frictional plane)",
         "config": {"workload": f"single {a.side}^3 lattice, {nm} masses, {ns} springs, 20% actuated, "
                                "plane + ball, dt=1e-4", "masses": nm, "springs": ns,
                    "precision": a.precision, "parallelism": "replicas" if world > 1 else "single GPU",
@@ -343,7 +343,7 @@ def run_reference(a, rank, world):
         return None
     from titan_gb300 import workloads as wl
     from oracle import pyoracle as po
-    sc = wl.config2(a.side)
+    sc = wl.actuated_lattice(a.side)
     ns = sc["left"].size
     threads = os.cpu_count() or 1
     o = po.OracleSim(sc)
@@ -355,7 +355,7 @@ def run_reference(a, rank, world):
     val = ns * k / dt
     return {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded lattice, BASELINE single-lattice configuration)",
+            "dtype": "f64", "data": "synthetic (seeded actuated lattice on a frictional plane)",
             "config": {"workload": f"single {a.side}^3 lattice, {sc['pos'].shape[0]} masses, {ns} springs, "
                                    "20% actuated, plane + ball, dt=1e-4", "precision": "f64"},
             "impl": "reference",
@@ -393,10 +393,10 @@ def run_suite(a, local):
     torch.cuda.set_device(local)
     threads = os.cpu_count() or 1
     rows = [
-        ("5^3 lattice, contact + friction (config 1 contact variant)", wl.config1(contact=True), 10000, 2000,
+        ("5^3 lattice, contact + friction (config 1 contact variant)", wl.falling_cube(contact=True), 10000, 2000,
          5000, 2000),
-        ("100^3 lattice, 20% actuated, plane + ball (config 2)", wl.config2(), 1000, 200, 50, 4),
-        ("4096 bodies, 3-12 masses per side, own planes (config 3)", wl.config3(nbodies=4096), 5000, 200, 20, 4),
+        ("100^3 lattice, 20% actuated, plane + ball (config 2)", wl.actuated_lattice(), 1000, 200, 50, 4),
+        ("4096 bodies, 3-12 masses per side, own planes (config 3)", wl.robot_batch(nbodies=4096), 5000, 200, 20, 4),
     ]
     for name, sc, steps, eng_steps, ref_steps, cpu_steps in rows:
         ns, nm = sc["left"].size, sc["pos"].shape[0]
@@ -452,7 +452,7 @@ def run_precision_study(a, local):
     from titan_gb300 import workloads as wl
 
     torch.cuda.set_device(local)
-    sc = wl.config4()
+    sc = wl.settling_lattice()
     n = sc["pos"].shape[0]
     chunk = max(1, a.study_steps // 10)
     sims = {p: wl.make_sim(sc, p, 0, device=local) for p in (tg.FP64, tg.FP32, tg.FP32C)}
@@ -506,7 +506,7 @@ def run_serving(a, local):
 
     torch.cuda.set_device(local)
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
-    reqs = wl.config5(a.serve_requests, a.serve_rate, mass_range=(27, a.serve_max_masses))
+    reqs = wl.request_stream(a.serve_requests, a.serve_rate, mass_range=(27, a.serve_max_masses))
     # scenes built before the clock starts (request payloads arrive ready)
     scenes = {r["id"]: wl.rollout_request(r["side"], r["seed"]) for r in reqs}
     srv = serving.RolloutServer(prec, device=local, small_masses=a.serve_small_masses)

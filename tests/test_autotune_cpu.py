@@ -28,7 +28,7 @@ def timings(monkeypatch):
 
 
 def test_fastest_candidate_is_chosen_and_cached(timings, tmp_path):
-    sc = wl.config2(n_side=10)
+    sc = wl.actuated_lattice(n_side=10)
     cache = tmp_path / "tune.json"
     cands = [(4, 208, 448), (4, 192, 448), (3, 999, 256), (1, 256, 256)]
     best = at.autotune(sc, tg.FP32C, candidates=cands, cache_path=cache)
@@ -46,7 +46,7 @@ def test_fastest_candidate_is_chosen_and_cached(timings, tmp_path):
 
 
 def test_keys_separate_scenes_and_precisions(timings, tmp_path):
-    a, b = wl.config2(n_side=10), wl.config2(n_side=12)
+    a, b = wl.actuated_lattice(n_side=10), wl.actuated_lattice(n_side=12)
     assert at.scene_key(a, tg.FP32C) != at.scene_key(b, tg.FP32C)
     assert at.scene_key(a, tg.FP32C) != at.scene_key(a, tg.FP64)
     cache = tmp_path / "tune.json"
@@ -58,11 +58,11 @@ def test_keys_separate_scenes_and_precisions(timings, tmp_path):
 
 def test_no_candidate_fits_raises(timings, tmp_path):
     with pytest.raises(RuntimeError, match="no launch configuration ran"):
-        at.autotune(wl.config2(n_side=8), tg.FP32C, candidates=[(2, 7, 7)], cache_path=tmp_path / "t.json")
+        at.autotune(wl.actuated_lattice(n_side=8), tg.FP32C, candidates=[(2, 7, 7)], cache_path=tmp_path / "t.json")
 
 
 def test_corrupt_cache_is_rebuilt(timings, tmp_path):
     cache = tmp_path / "tune.json"
     cache.write_text("{not json")
-    best = at.autotune(wl.config2(n_side=8), tg.FP32C, candidates=[(1, 256, 256)], cache_path=cache)
+    best = at.autotune(wl.actuated_lattice(n_side=8), tg.FP32C, candidates=[(1, 256, 256)], cache_path=cache)
     assert best["kernel"] == 1 and json.loads(cache.read_text())

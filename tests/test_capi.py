@@ -202,7 +202,7 @@ def test_plan_default_tile_adapts_and_keeps_small_bodies_whole():
     P = plan_tables(small, 0)
     nm = np.diff(P["tile_mass_off"])
     assert nm.max() <= 128 and P["tile_mass_off"].size - 1 >= 60
-    sc = wl.config3(nbodies=40, seed=3, side_range=(3, 7))
+    sc = wl.robot_batch(nbodies=40, seed=3, side_range=(3, 7))
     P = plan_tables(sc, 0)
     bp = sc["body_ptr"]
     sizes = np.diff(bp)
@@ -273,7 +273,7 @@ def test_plan_slab_groups_avoid_bank_conflicts():
     """The planner orders each tile's slab so that a quarter-warp's endpoint
     records mostly fall in distinct bank groups (spring order alone gives
     about 1.6-1.7 wavefronts per load on a lattice)."""
-    sc = wl.config2(n_side=16)
+    sc = wl.actuated_lattice(n_side=16)
     P = plan_tables(sc, 192)
     assert bank_wavefronts(P) < 1.2
 
@@ -281,7 +281,7 @@ def test_plan_slab_groups_avoid_bank_conflicts():
 def test_plan_is_deterministic():
     """The planner orders tile slabs on several host threads; two plans of
     the same scene are the same, table for table."""
-    sc = wl.config3(nbodies=48, seed=11, side_range=(3, 9))
+    sc = wl.robot_batch(nbodies=48, seed=11, side_range=(3, 9))
     wl.actuate(sc, np.random.default_rng(4), 0.3, 0.1)
     a, b = plan_tables(sc, 0), plan_tables(sc, 0)
     for k in a:
@@ -296,7 +296,7 @@ def test_plan_heavy_hub():
 
 
 def test_plan_bodies():
-    sc = wl.config3(nbodies=12, seed=4, side_range=(3, 6))
+    sc = wl.robot_batch(nbodies=12, seed=4, side_range=(3, 6))
     validate(sc, plan_tables(sc, 64))
 
 
@@ -394,14 +394,14 @@ def validate_resident(sc, R, cap):
 
 
 def test_resident_plan_bins():
-    sc = wl.config3(nbodies=30, seed=5, side_range=(3, 7))
+    sc = wl.robot_batch(nbodies=30, seed=5, side_range=(3, 7))
     rng = np.random.default_rng(1)
     sc["fixed"] = (rng.random(sc["pos"].shape[0]) < 0.05).astype(np.uint8)
     validate_resident(sc, resident_tables(sc, (1, 512, 0)), 512)
 
 
 def test_resident_plan_excludes_large_and_coupled_bodies():
-    sc = wl.config3(nbodies=16, seed=6, side_range=(3, 8))
+    sc = wl.robot_batch(nbodies=16, seed=6, side_range=(3, 8))
     bp = sc["body_ptr"]
     # a spring between bodies 0 and 1 keeps both on the per-step kernels
     for key, val in (("left", bp[0]), ("right", bp[1]), ("k", 1e3), ("rest", 1.0), ("damping", 0.0), ("type", 0),

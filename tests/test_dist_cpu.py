@@ -31,7 +31,7 @@ def _rank(rank, world, port, out):
                       LOCAL_RANK=str(rank))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     assert bench.dist_env() == (rank, world, rank)
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     o = po.OracleSim(sc)
     t0 = time.perf_counter()
     o.step(200 + 100 * rank, po.ASCENDING, 1)  # unequal work: rank 1 is slower

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("precision", [tg.FP64, tg.FP32, tg.FP32C])
 def test_export_vertices_host_and_device(precision):
     import torch
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s = wl.make_sim(sc, precision)
     s.step(123)
     pos = s.get_state(pos=True, vel=False)["pos"]
@@ -29,7 +29,7 @@ def test_export_vertices_host_and_device(precision):
 
 
 def test_poll_and_bounded_wait():
-    sc = wl.config2(40)
+    sc = wl.actuated_lattice(40)
     s = wl.make_sim(sc, tg.FP32C)
     s.synchronize()
     assert s.poll()

@@ -235,7 +235,7 @@ def test_orders_differ_only_by_rounding():
     rounding difference to ~1e-5 m within 0.1 s: that spread is the
     reference's own run-to-run nondeterminism in contact."""
     from titan_gb300 import workloads as wl
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     sc["vel"] = np.random.default_rng(1).normal(scale=0.3, size=sc["pos"].shape)
     a, b = po.OracleSim(sc), po.OracleSim(sc)
     a.step(1, po.ASCENDING)
@@ -251,7 +251,7 @@ def test_orders_differ_only_by_rounding():
 
 def test_device_order_is_ascending_without_heavy_masses():
     from titan_gb300 import workloads as wl
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     a, b = po.OracleSim(sc), po.OracleSim(sc)
     a.step(300, po.ASCENDING)
     b.step(300, po.DEVICE, nthreads=2)

@@ -43,16 +43,16 @@ def assert_bitwise(st, o):
     assert np.array_equal(st["T"], o.T)
 
 
-def test_config1_free_fall_10k_steps_bitwise():
-    sc = wl.config1()
+def test_falling_cube_free_fall_10k_steps_bitwise():
+    sc = wl.falling_cube()
     s, st = gpu_run(sc, 10000)
     o = oracle_run(sc, 10000)
     assert_bitwise(st, o)
     assert s.time == o.time
 
 
-def test_config1_contact_friction_10k_steps_bitwise():
-    sc = wl.config1(contact=True)
+def test_falling_cube_contact_friction_10k_steps_bitwise():
+    sc = wl.falling_cube(contact=True)
     sc["vel"] = np.random.default_rng(1).normal(scale=0.3, size=sc["pos"].shape)
     _, st = gpu_run(sc, 10000)
     o = oracle_run(sc, 10000)
@@ -111,7 +111,7 @@ def test_heavy_hub_device_order_bitwise():
 
 
 def test_bodies_with_own_planes_bitwise():
-    sc = wl.config3(nbodies=24, seed=9, side_range=(3, 7))
+    sc = wl.robot_batch(nbodies=24, seed=9, side_range=(3, 7))
     for key in ("type",):
         sc[key][:] = 0  # passive: bitwise bar
     _, st = gpu_run(sc, 3000, tile=128, resident=(0, 0, 0))
@@ -147,7 +147,7 @@ def kernel_scenes():
     wl.actuate(lat, rng, 0.3, 0.1)
     lat["planes"].append(((0.0, 0.1, 1.0), 0.0, 0.4, 0.6))
     lat["balls"].append(((0.3, 0.0, -0.1), 0.35))
-    return {"lattice": lat, "hub": hub_scene(degree=300), "bodies": wl.config3(nbodies=24, seed=9, side_range=(3, 7))}
+    return {"lattice": lat, "hub": hub_scene(degree=300), "bodies": wl.robot_batch(nbodies=24, seed=9, side_range=(3, 7))}
 
 
 @pytest.mark.parametrize("precision", [tg.FP64, tg.FP32, tg.FP32C])
@@ -184,7 +184,7 @@ def test_pipelined_kernel_with_few_ctas_per_tile_list():
 
 
 def test_graph_chunks_equal_single_steps_and_repeatable():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     _, a = gpu_run(sc, 777)
     _, b = gpu_run(sc, 777, chunks=[1] * 77 + [100, 600])
     _, c = gpu_run(sc, 777)
@@ -193,7 +193,7 @@ def test_graph_chunks_equal_single_steps_and_repeatable():
 
 
 def test_state_roundtrip_and_partial_set():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s = wl.make_sim(sc)
     s.step(500)
     st = s.get_state(acc=True, T=True)
@@ -213,7 +213,7 @@ def test_state_roundtrip_and_partial_set():
 
 
 def test_fix_after_start_rebuilds_plan():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s = wl.make_sim(sc)
     o = po.OracleSim(sc)
     s.step(200)
@@ -230,7 +230,7 @@ def test_fix_after_start_rebuilds_plan():
 
 
 def test_spring_param_update():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s = wl.make_sim(sc)
     s.step(100)
     o = oracle_run(sc, 100)
@@ -243,7 +243,7 @@ def test_spring_param_update():
 
 
 def test_diagnostics_match_oracle():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s, st = gpu_run(sc, 3000)
     o = oracle_run(sc, 3000)
     d = s.diagnostics(9.8)
@@ -265,7 +265,7 @@ def test_fp32c_error_free_flight_10k_steps():
     """No contact (config 1 as given: the lattice never reaches the plane):
     FP32C stays under 1e-5 m of FP64 after 10^4 steps; plain FP32 does not
     need to."""
-    sc = wl.config1()
+    sc = wl.falling_cube()
     err_c, err_f = fp_errors(sc, 10000)
     print(f"free flight 10^4 steps: fp32c {err_c:.3e} m, fp32 {err_f:.3e} m")
     assert err_c < 1e-5
@@ -278,7 +278,7 @@ def test_fp32c_contact_statistics_against_fp64():
     bound is meaningless there.  FP32C must agree with FP64 in the
     statistics: total energy within 0.5% after 10^4 steps of the contact
     scene.  The pointwise errors are printed for the record."""
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     s64, ref = gpu_run(sc, 10000, tg.FP64)
     s32, c = gpu_run(sc, 10000, tg.FP32C)
     oa, od = oracle_run(sc, 10000), oracle_run(sc, 10000, po.DESCENDING)
@@ -290,11 +290,11 @@ def test_fp32c_contact_statistics_against_fp64():
     assert abs(e32 - e64) <= 5e-3 * abs(e64)
 
 
-def test_full_size_config2_fp64_matches_oracle_three_steps():
-    """BASELINE single-lattice workload at full size (100^3 masses, 12.7M
+def test_full_size_actuated_lattice_fp64_matches_oracle_three_steps():
+    """The single-lattice workload at full size (100^3 masses, 12.7M
     springs, 20% actuated): three FP64 steps against the oracle (parallel,
     device order), 1e-12 relative on velocities; positions finite."""
-    sc = wl.config2()
+    sc = wl.actuated_lattice()
     s = wl.make_sim(sc, tg.FP64)
     s.step(3)
     st = s.get_state()
@@ -305,8 +305,8 @@ def test_full_size_config2_fp64_matches_oracle_three_steps():
     assert np.max(np.abs(st["pos"] - o.pos)) <= 1e-12 * np.max(np.abs(o.pos))
 
 
-def test_full_size_config2_fp32c_vs_fp64_200_steps():
-    sc = wl.config2()
+def test_full_size_actuated_lattice_fp32c_vs_fp64_200_steps():
+    sc = wl.actuated_lattice()
     _, a = gpu_run(sc, 200, tg.FP64)
     _, b = gpu_run(sc, 200, tg.FP32C)
     assert np.all(np.isfinite(b["pos"]))

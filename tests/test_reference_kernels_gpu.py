@@ -54,7 +54,7 @@ def compare(sc, nsteps, bound):
 
 
 def test_contact_friction_lattice_per_step():
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     sc["vel"] = np.random.default_rng(1).normal(scale=0.3, size=sc["pos"].shape)
     compare(sc, 1, 1e-9)
 
@@ -86,5 +86,5 @@ def test_free_flight_1000_steps():
 def test_full_size_single_lattice_three_steps():
     """100^3 lattice (1,000,000 masses, 12,731,796 springs), plane and ball,
     20% actuated at the reference's amplitude."""
-    sc = reference_actuation(wl.config2())
+    sc = reference_actuation(wl.actuated_lattice())
     compare(sc, 3, 1e-9)

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def batch(nbodies=40, seed=12, side_range=(3, 7), passive=True):
-    sc = wl.config3(nbodies=nbodies, seed=seed, side_range=side_range)
+    sc = wl.robot_batch(nbodies=nbodies, seed=seed, side_range=side_range)
     rng = np.random.default_rng(seed)
     n = sc["pos"].shape[0]
     if passive:
@@ -162,7 +162,7 @@ def test_resident_tiles_single_body_with_contact(precision):
     """The small-robot scene (one actuated 125-mass lattice on a friction
     plane): one resident tile with its records staged in shared memory,
     bit-identical to the per-step kernels over calls of any length."""
-    sc = wl.actuate(wl.config1(contact=True), np.random.default_rng(7), 0.3, 0.1)
+    sc = wl.actuate(wl.falling_cube(contact=True), np.random.default_rng(7), 0.3, 0.1)
     chunks = [1, 63, 200, 2000]
     s1, a = run(sc, chunks, precision, resident=(2, 0, 0))
     i1 = s1.resident_info()
@@ -188,7 +188,7 @@ def test_automatic_resident_tiles_choice():
     """By default resident tiles carry the halo-free tiles (symplectic
     Euler, automatic kernel form): a whole small scene, the small bodies of
     a batch beside the per-step kernels, nothing of a single large lattice."""
-    small = wl.config1(contact=True)
+    small = wl.falling_cube(contact=True)
     s = wl.make_sim(small, tg.FP32C)
     assert s.resident_info()["active"] == 2 and s.plan_info()["tiles"] == 1
     assert s.kernel_info()["kernel"] == "resident-tiles" and s.kernel_info()["ctas"] == 1
@@ -196,7 +196,7 @@ def test_automatic_resident_tiles_choice():
     s = wl.make_sim(small, tg.FP32C, kernel=1)  # an explicit kernel form: per-step kernels
     assert s.resident_info()["active"] == 0
     s.close()
-    s = wl.make_sim(wl.config2(n_side=20), tg.FP32C)  # tiles with halos
+    s = wl.make_sim(wl.actuated_lattice(n_side=20), tg.FP32C)  # tiles with halos
     assert s.resident_info()["active"] == 0
     s.close()
     mixed = batch(nbodies=24, seed=21, side_range=(3, 9), passive=False)  # 9^3 bodies span several tiles
@@ -219,7 +219,7 @@ def test_automatic_resident_tiles_choice():
 def test_set_integrator_leaves_resident_tiles_bitwise():
     """A switch to RK2 after some Euler steps rebuilds the scene on the
     per-step kernels: same bits as a run that never had resident tiles."""
-    sc = wl.actuate(wl.config1(contact=True), np.random.default_rng(8), 0.3, 0.1)
+    sc = wl.actuate(wl.falling_cube(contact=True), np.random.default_rng(8), 0.3, 0.1)
     out = []
     for res in ((2, 0, 0), (0, 0, 0)):
         s = wl.make_sim(sc, tg.FP64, 128, resident=res)  # the body in one tile

@@ -48,7 +48,7 @@ def test_admission_by_budget_serialises():
 
 
 def test_poisson_arrivals_complete():
-    reqs = wl.config5(40, rate=400.0, mass_range=(27, 3000), horizon=(100, 400))
+    reqs = wl.request_stream(40, rate=400.0, mass_range=(27, 3000), horizon=(100, 400))
     srv = serving.RolloutServer(tg.FP32C)
     recs, stats = srv.run(reqs)
     srv.close()

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("precision", [tg.FP64, tg.FP32C])
 def test_pinned_and_pageable_paths_agree(precision):
-    sc = wl.config2(n_side=24)
+    sc = wl.actuated_lattice(n_side=24)
     n = sc["pos"].shape[0]
     rng = np.random.default_rng(3)
     pos = sc["pos"] + rng.normal(scale=1e-3, size=(n, 3))

@@ -38,7 +38,7 @@ def test_noalloc_diagnostics_match_handle_entry_point():
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", 0)
     fn = noalloc_fn()
-    sc = wl.config1(contact=True)
+    sc = wl.falling_cube(contact=True)
     sc["vel"] = np.random.default_rng(7).normal(scale=0.2, size=sc["pos"].shape)
     sim = wl.make_sim(sc, tg.FP64)
     left = torch.tensor(sc["left"], dtype=torch.int32, device=dev)

@@ -25,6 +25,8 @@ PKG = ROOT / "titan_gb300"
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 ORACLE = ROOT / "oracle"
+# the reference sources the oracle pin compiles from (oracle/build_ref.sh reads the same variable)
+REFERENCE = Path(os.environ.get("TITAN_REFERENCE", "/root/reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: every kernel rounds each product and sum separately, as the
@@ -122,7 +124,7 @@ def build_reference_pieces(verbose: bool = False) -> Path | None:
     """Compile the reference's host-callable code into oracle/_ref (only where
     the reference sources exist; the recipe is oracle/build_ref.sh)."""
     script = ORACLE / "build_ref.sh"
-    if not Path("/root/reference/src/object.cu").exists() or not script.exists():
+    if not (REFERENCE / "src" / "object.cu").exists() or not script.exists():
         return None
     out = ORACLE / "_ref" / "libtitan_ref_host.so"
     deps = [script, ORACLE / "ref_host_shim.cu", ORACLE / "ref_gpu_shim.cu", *(ORACLE / "ref_shims").glob("*.h")]

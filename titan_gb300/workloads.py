@@ -37,7 +37,7 @@ def lattice_scene(center, dims, nx, ny, nz, m=0.1, k=1e4, damping=0.0, dt=1e-4, 
     return sc
 
 
-def config1(contact=False):
+def falling_cube(contact=False):
     """5x5x5 lattice of 0.1 kg masses spanning 5 m, centre (0,0,10), k=1e4,
     no damping, g=(0,0,-9.81), plane z=0 with friction (mu_k = mu_s = 0.5, the
     friction values are not given by the configuration), dt=1e-4.
@@ -62,7 +62,7 @@ def actuate(sc, rng, fraction, amp, period=(0.1, 1.0), kinds=(2, 3)):
     return sc
 
 
-def config2(n_side=100, seed=20261203):
+def actuated_lattice(n_side=100, seed=20261203):
     """Single large lattice: n_side^3 masses (100^3 = 1,000,000 masses,
     12,731,796 springs), 5 m cube centred at (0,0,2.6) so its bottom face
     starts 0.1 m above the plane, m = 0.1 kg; k log-uniform in [1e3, 1e5],
@@ -82,7 +82,7 @@ def config2(n_side=100, seed=20261203):
     return sc
 
 
-def config4(n_side=64, seed=7):
+def settling_lattice(n_side=64, seed=7):
     """Long-horizon study scene: n_side^3 lattice (64^3 = 262,144 masses) of
     0.1 kg masses spanning 3 m, dropped from 0.05 m onto a frictional plane
     (mu 0.5), k = 1e4, damping 0.1, dt = 1e-5."""
@@ -111,7 +111,7 @@ def body_lattice(side, spacing, center, rng, drop=0.05, act_fraction=0.3, amp=0.
     return pos, left, right, rest, k, typ, ampa, ph, om
 
 
-def config3(nbodies=4096, seed=3, side_range=(3, 12), spacing=0.1, pitch=2.0):
+def robot_batch(nbodies=4096, seed=3, side_range=(3, 12), spacing=0.1, pitch=2.0):
     """Batch of independent soft-body robots: side ~ U{3..12} masses per axis
     (0.1 m spacing, 0.1 kg masses), 5% of springs removed per body, k
     log-uniform in [1e3, 1e5], damping 0.1, 30% actuated (amplitude 0.1,
@@ -238,7 +238,7 @@ def rollout_request(side, seed, dt=1e-4):
     return sc
 
 
-def config5(nreq, rate, seed=5, mass_range=(27, 200000), horizon=(100, 5000)):
+def request_stream(nreq, rate, seed=5, mass_range=(27, 200000), horizon=(100, 5000)):
     """Serving workload: nreq rollout requests with Poisson arrivals at `rate`
     per second, masses log-uniform in mass_range (cube side =
     round(cbrt(masses))), horizon U[horizon] steps.  Returns a list of dicts
