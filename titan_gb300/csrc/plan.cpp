@@ -151,14 +151,6 @@ void bank_order(std::vector<int64_t> &v, const std::vector<uint32_t> &ls, const 
     v.swap(out);
 }
 
-// Permutes the entries inside each aligned group of eight slab positions
-// (never across the actuated / non-actuated boundary), which keeps the
-// grouping above, so that the force slots one quarter-warp gathers at one
-// incidence position -- the j-th codes of eight consecutive masses, 16-byte
-// loads of slots at bank group (slot mod 8) -- fall in distinct bank groups
-// where they can.  Greedy per group: the entries with the most gather
-// references first, each to the free position whose residue the entry's
-// (quarter-warp, j) sets use least.
 // Scratch of the slab ordering, reused from tile to tile: a spring -> slab
 // position table (open addressing; a slot is live when its stamp is the
 // current round's) and the per-entry and per-set arrays of gather_permute.
@@ -168,9 +160,9 @@ struct PermuteScratch {
     std::vector<uint32_t> hstamp;
     uint32_t stamp = 0;
     int64_t hcap = 0;
-    std::vector<int64_t> seq, out;
-    std::vector<int32_t> k0, k1;
-    std::vector<uint8_t> cnt;
+    std::vector<int64_t> seq;
+    std::vector<int32_t> at, k0, k1;
+    std::vector<uint8_t> cnt, mx;
 
     void begin(int64_t ne) {  // an empty table for up to ne springs
         int64_t c = 16;
@@ -199,6 +191,97 @@ struct PermuteScratch {
     int32_t get(int64_t sp) const { return hval[probe(sp)]; }
 };
 
+// Lowers the gather cost of a slab's within-group permutation by pairwise
+// swaps.  A set (one quarter-warp's force loads at one incidence position)
+// costs the most entries it reads from one bank group -- its wavefronts;
+// two entries of one group (and one part) trade positions when that lowers
+// the summed cost of their sets.  at: position -> entry; k0/k1: the entry's
+// sets (-1: none); cnt: per set and residue, the entries read; mx:
+// scratch for the sets' costs.  Sweeps over the groups repeat while one
+// changes something, at most kSweeps times.
+void swap_search(std::vector<int32_t> &at, const std::vector<int32_t> &k0, const std::vector<int32_t> &k1,
+                 std::vector<uint8_t> &cnt, std::vector<uint8_t> &mx, int64_t na) {
+    constexpr int kSweeps = 2;
+    const int64_t ne = (int64_t)at.size(), nsets = (int64_t)(cnt.size() / 8);
+    mx.resize((size_t)nsets);  // per set, its cost: the largest count
+    for (int64_t st = 0; st < nsets; st++) mx[st] = *std::max_element(&cnt[st * 8], &cnt[st * 8] + 8);
+    // change of a set's cost when one of its entries moves from residue
+    // `from` to `to`: up when `to` is at the maximum, down when `from` is
+    // the only residue at it and `to` stays below it
+    auto delta = [&](int32_t st, int from, int to) {
+        const uint8_t *c = &cnt[(size_t)st * 8];
+        const int m = mx[st];
+        if (c[to] == m) return 1;
+        if (c[from] != m || c[to] + 1 == m) return 0;
+        for (int r = 0; r < 8; r++)
+            if (r != from && c[r] == m) return 0;
+        return -1;
+    };
+    auto move = [&](int32_t st, int from, int to) {
+        uint8_t *c = &cnt[(size_t)st * 8];
+        c[from]--;
+        c[to]++;
+        mx[st] = *std::max_element(c, c + 8);
+    };
+    for (int sweep = 0; sweep < kSweeps; sweep++) {
+        bool changed = false;
+        for (int64_t b0 = 0; b0 < ne; b0 += 8) {
+            const int64_t b1 = std::min<int64_t>(b0 + 8, ne);
+            for (int side = 0; side < 2; side++) {
+                const int64_t s0 = side == 0 ? b0 : std::max(b0, na), s1 = side == 0 ? std::min(b1, na) : b1;
+                if (s1 - s0 < 2) continue;
+                // a swap lowers the cost only if one of its entries is the
+                // only one at the maximum (of 2 or more) of one of its sets
+                bool drop[8];
+                auto mark = [&]() {
+                    for (int64_t p = s0; p < s1; p++) {
+                        drop[p - s0] = false;
+                        for (int32_t st : {k0[at[p]], k1[at[p]]}) {
+                            if (st < 0) continue;
+                            const uint8_t *c = &cnt[(size_t)st * 8];
+                            if (mx[st] < 2 || c[p & 7] != mx[st]) continue;
+                            int at_max = 0;
+                            for (int r = 0; r < 8; r++) at_max += c[r] == mx[st];
+                            drop[p - s0] = drop[p - s0] || at_max == 1;
+                        }
+                    }
+                };
+                mark();
+                for (int64_t p = s0; p < s1; p++)
+                    for (int64_t q = p + 1; q < s1; q++) {
+                        if (!drop[p - s0] && !drop[q - s0]) continue;
+                        const int32_t x = at[p], y = at[q];
+                        const int rp = (int)(p & 7), rq = (int)(q & 7);
+                        const int32_t sx[2] = {k0[x], k1[x]}, sy[2] = {k0[y], k1[y]};
+                        auto in = [](const int32_t *v, int32_t st) { return v[0] == st || v[1] == st; };
+                        int d = 0;  // a set holding both entries keeps its counts
+                        for (int32_t st : sx)
+                            if (st >= 0 && !in(sy, st)) d += delta(st, rp, rq);
+                        for (int32_t st : sy)
+                            if (st >= 0 && !in(sx, st)) d += delta(st, rq, rp);
+                        if (d >= 0) continue;
+                        for (int32_t st : sx)
+                            if (st >= 0 && !in(sy, st)) move(st, rp, rq);
+                        for (int32_t st : sy)
+                            if (st >= 0 && !in(sx, st)) move(st, rq, rp);
+                        std::swap(at[p], at[q]);
+                        changed = true;
+                        mark();
+                    }
+            }
+        }
+        if (!changed) break;
+    }
+}
+
+// Permutes the entries inside each aligned group of eight slab positions
+// (never across the actuated / non-actuated boundary), which keeps the
+// grouping above, so that the force slots one quarter-warp gathers at one
+// incidence position -- the j-th codes of eight consecutive masses, 16-byte
+// loads of slots at bank group (slot mod 8) -- fall in distinct bank groups
+// where they can.  Greedy per group first: the entries with the most gather
+// references first, each to the free position whose residue the entry's
+// (quarter-warp, j) sets use least; then swap_search.
 void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64_t lo, int64_t hi,
                     const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t heavy_threshold,
                     PermuteScratch &W) {
@@ -216,6 +299,7 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
         const int64_t d = ip[m + 1] - ip[m];
         if (d <= heavy_threshold) maxd = std::max(maxd, d);
     }
+    maxd = (maxd + 3) & ~int64_t(3);  // incidence positions, padding included
     // the (quarter-warp, incidence position) sets each entry belongs to
     std::vector<int32_t> &k0 = W.k0, &k1 = W.k1;
     k0.assign((size_t)ne, -1);
@@ -226,13 +310,23 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
         for (int64_t j = 0; j < d; j++) {
             const int64_t p = W.get(isp[ip[m] + j]);
             const int32_t key = (int32_t)(((m - lo) >> 3) * maxd + j);
-            (k0[p] < 0 ? k0[p] : k1[p]) = key;
+            if (k0[p] < 0) k0[p] = key;
+            else if (k0[p] != key) k1[p] = key;  // both ends in one set: one broadcast load
         }
     }
     std::vector<uint8_t> &cnt = W.cnt;
     cnt.assign((size_t)(((nm + 7) >> 3) * maxd * 8), 0);
-    std::vector<int64_t> &out = W.out;
-    out.assign(seq.begin(), seq.end());
+    // a mass's codes past its degree, up to a whole word of four, are
+    // padding that the padded gathers load from slot ne: one fixed (and
+    // broadcast) slot of those sets
+    for (int64_t m = lo; m < hi; m++) {
+        const int64_t d = ip[m + 1] - ip[m];
+        if (d > heavy_threshold) continue;
+        for (int64_t j = d; j < ((d + 3) & ~int64_t(3)); j++)
+            cnt[(size_t)((((m - lo) >> 3) * maxd + j) * 8 + (ne & 7))] = 1;
+    }
+    std::vector<int32_t> &at = W.at;  // position -> entry (index into seq)
+    at.assign((size_t)ne, 0);
     for (int64_t b0 = 0; b0 < ne; b0 += 8) {
         const int64_t b1 = std::min<int64_t>(b0 + 8, ne);
         for (int side = 0; side < 2; side++) {
@@ -264,12 +358,106 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
                 const int r = (int)((s0 + best) & 7);
                 if (k0[x] >= 0) cnt[(size_t)k0[x] * 8 + r]++;
                 if (k1[x] >= 0) cnt[(size_t)k1[x] * 8 + r]++;
-                out[s0 + best] = seq[x];
+                at[s0 + best] = (int32_t)x;
             }
         }
     }
-    act.assign(out.begin(), out.begin() + na);
-    rest.assign(out.begin() + na, out.end());
+    swap_search(at, k0, k1, cnt, W.mx, na);
+    act.resize((size_t)na);
+    rest.resize((size_t)(ne - na));
+    for (int64_t p = 0; p < ne; p++) (p < na ? act[p] : rest[p - na]) = seq[at[p]];
+}
+
+// Runs f(state, i) for every i in [0, count) on up to 16 host threads, each
+// with its own State; at least `grain` items per thread.  f may write only
+// what belongs to item i.
+template <class State, class F>
+void parallel_items(int64_t count, int64_t grain, F &&f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), std::max<int64_t>(1, count / grain));
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        State state;
+        for (int64_t i; (i = next.fetch_add(1)) < count;) f(state, i);
+    };
+    std::vector<std::thread> pool;
+    for (int q = 1; q < nt; q++) pool.emplace_back(worker);
+    worker();
+    for (auto &th : pool) th.join();
+}
+
+// One tile of the layout: masses [lo, hi); its slab entries (every spring
+// that a free mass of the tile is an end of, once) in ascending spring
+// order, actuated ones apart; the other ends outside the tile (its halo),
+// ascending.
+struct TileLayout {
+    int64_t lo = 0, hi = 0;
+    std::vector<int64_t> act, rest;
+    std::vector<int32_t> halo;
+};
+
+// The tiles of one leaf: the leaf itself while its slab, halo and
+// state records fit the tile limits, else its two halves (first half
+// first, recursively).  err: a single mass whose slab does not fit.
+struct LeafLayout {
+    std::vector<TileLayout> tiles;
+    std::string err;
+};
+
+struct LayoutScratch {
+    std::vector<int64_t> ents;
+    std::vector<int32_t> halo;
+};
+
+void layout_leaf(const PlanInput &in, const Plan &P, const std::vector<int32_t> &L, const std::vector<int32_t> &R,
+                 const std::vector<int64_t> &ip, const std::vector<int64_t> &isp, int64_t lo0, int64_t hi0,
+                 LeafLayout &out, LayoutScratch &S) {
+    out.tiles.clear();
+    out.err.clear();
+    std::deque<std::pair<int64_t, int64_t>> work{{lo0, hi0}};
+    while (!work.empty()) {
+        const auto [lo, hi] = work.front();
+        work.pop_front();
+        const int64_t nm = hi - lo;
+        // the incidence of masses lo..hi-1 is one range of isp
+        S.ents.assign(isp.begin() + ip[lo], isp.begin() + ip[hi]);
+        std::sort(S.ents.begin(), S.ents.end());
+        S.ents.erase(std::unique(S.ents.begin(), S.ents.end()), S.ents.end());
+        const int64_t ne = (int64_t)S.ents.size();
+        bool fits = ne <= in.entry_cap;
+        if (fits) {
+            S.halo.clear();
+            for (int64_t sp : S.ents)
+                for (int32_t x : {L[sp], R[sp]})
+                    if (x < lo || x >= hi) S.halo.push_back(x);
+            std::sort(S.halo.begin(), S.halo.end());
+            S.halo.erase(std::unique(S.halo.begin(), S.halo.end()), S.halo.end());
+            fits = nm + (int64_t)S.halo.size() <= in.slot_cap;
+            if (fits) {
+                int64_t heavy = 0;
+                for (int64_t m = lo; m < hi; m++) heavy += (ip[m + 1] - ip[m]) > in.heavy_threshold;
+                fits = (nm + (int64_t)S.halo.size()) * in.slot_bytes + (ne + 1) * in.entry_bytes +
+                           heavy * in.heavy_bytes <= in.smem_budget;
+            }
+        }
+        if (!fits) {
+            if (nm == 1) {
+                out.err = "mass " + std::to_string(P.new2old[lo]) + " has " + std::to_string(ip[lo + 1] - ip[lo]) +
+                          " springs, more than one tile's slab can hold";
+                return;
+            }
+            const int64_t mid = lo + nm / 2;
+            work.emplace_front(mid, hi);
+            work.emplace_front(lo, mid);
+            continue;
+        }
+        TileLayout t;
+        t.lo = lo;
+        t.hi = hi;
+        for (int64_t sp : S.ents) (actuated(in, sp) ? t.act : t.rest).push_back(sp);
+        t.halo = S.halo;
+        out.tiles.push_back(std::move(t));
+    }
 }
 
 // Final slab order of tile t (bank_order on each part, then
@@ -446,12 +634,8 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     }
 
     // ---- tiles ------------------------------------------------------------
-    std::vector<int64_t> smark(ns, -1);
-    std::vector<int64_t> hmark(n, -1);
-    std::vector<int64_t> ents, ents_act;
-    std::vector<int32_t> halo;
-    int64_t attempt = 0;
-
+    // Leaves are laid out on several threads, a batch at a time (bounded
+    // memory), and their tiles appended to the tables in leaf order.
     P.tile_mass_off.push_back(0);
     P.tile_halo_off.push_back(0);
     P.tile_ent_off.push_back(0);
@@ -459,106 +643,81 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     P.tile_heavy_off.push_back(0);
     P.deg.assign(n, 0);
 
-    size_t leaf = 0;
-    for (int64_t b = 0; b < P.nbodies; b++) {
-        std::deque<std::pair<int64_t, int64_t>> work;
-        for (; leaf < leaf_end.size() && leaf_end[leaf] <= bptr[b + 1]; leaf++)
-            work.emplace_back(leaf == 0 ? 0 : leaf_end[leaf - 1], leaf_end[leaf]);
-        while (!work.empty()) {
-            auto [lo, hi] = work.front();
-            work.pop_front();
-            const int64_t nm = hi - lo;
-            attempt++;
-            ents.clear();
-            ents_act.clear();
-            halo.clear();
-            for (int64_t m = lo; m < hi; m++)
-                for (int64_t q = ip[m]; q < ip[m + 1]; q++) {
-                    int64_t s = isp[q];
-                    if (smark[s] == attempt) continue;
-                    smark[s] = attempt;
-                    (actuated(in, s) ? ents_act : ents).push_back(s);
-                }
-            int64_t ne = (int64_t)(ents.size() + ents_act.size());
-            bool fits = ne <= in.entry_cap;
-            if (fits) {
-                for (auto *v : {&ents_act, &ents})
-                    for (int64_t s : *v)
-                        for (int32_t x : {L[s], R[s]})
-                            if ((x < lo || x >= hi) && hmark[x] != attempt) {
-                                hmark[x] = attempt;
-                                halo.push_back(x);
-                            }
-                fits = nm + (int64_t)halo.size() <= in.slot_cap;
-                if (fits) {
-                    int64_t heavy = 0;
-                    for (int64_t m = lo; m < hi; m++) heavy += (ip[m + 1] - ip[m]) > in.heavy_threshold;
-                    fits = (nm + (int64_t)halo.size()) * in.slot_bytes + (ne + 1) * in.entry_bytes +
-                               heavy * in.heavy_bytes <= in.smem_budget;
-                }
-            }
-            if (!fits) {
-                if (nm == 1)
-                    return "mass " + std::to_string(P.new2old[lo]) + " has " +
-                           std::to_string(ip[lo + 1] - ip[lo]) +
-                           " springs, more than one tile's slab can hold";
-                int64_t mid = lo + nm / 2;
-                work.emplace_front(mid, hi);
-                work.emplace_front(lo, mid);
-                continue;
-            }
-            // commit the tile's layout; its slab order, entry words and
-            // incidence codes are filled in by order_tile() below
-            std::sort(ents_act.begin(), ents_act.end());
-            std::sort(ents.begin(), ents.end());
-            std::sort(halo.begin(), halo.end());
-            const int64_t nh = (int64_t)halo.size();
-            for (auto *v : {&ents_act, &ents}) P.ent_spring.insert(P.ent_spring.end(), v->begin(), v->end());
-            P.ent_ends.resize(P.ent_spring.size(), 0u);
-            P.halo.insert(P.halo.end(), halo.begin(), halo.end());
-            while (P.halo.size() % 4) P.halo.push_back(halo.empty() ? (int32_t)lo : halo.back());
-            P.tile_nh.push_back((int32_t)nh);
-            P.tile_nact.push_back((int32_t)ents_act.size());
+    const int64_t nleaves = (int64_t)leaf_end.size();
+    std::vector<int32_t> leaf_body((size_t)nleaves);
+    for (int64_t f = 0, b = 0; f < nleaves; f++) {
+        while (leaf_end[f] > bptr[b + 1]) b++;
+        leaf_body[f] = (int32_t)b;
+    }
+    // capacity: the tiles' entries are at most all incidences; the incidence
+    // blocks are about as many codes plus the padding of each warp's width
+    P.ent_spring.reserve((size_t)ip[n]);
+    P.ent_ends.reserve((size_t)ip[n]);
+    P.inc.reserve((size_t)(ip[n] + 4 * n));
+    constexpr int64_t kLeafBatch = 4096;
+    std::vector<LeafLayout> batch;
+    for (int64_t f0 = 0; f0 < nleaves; f0 += kLeafBatch) {
+        const int64_t nb = std::min(kLeafBatch, nleaves - f0);
+        batch.resize((size_t)nb);
+        parallel_items<LayoutScratch>(nb, 8, [&](LayoutScratch &S, int64_t i) {
+            const int64_t f = f0 + i;
+            layout_leaf(in, P, L, R, ip, isp, f == 0 ? 0 : leaf_end[f - 1], leaf_end[f], batch[i], S);
+        });
+        for (int64_t i = 0; i < nb; i++) {
+            if (!batch[i].err.empty()) return batch[i].err;
+            for (const TileLayout &T : batch[i].tiles) {
+                // the tile's slab order, entry words and incidence codes are
+                // filled in by order_tile() below
+                const int64_t lo = T.lo, hi = T.hi, nm = hi - lo;
+                const int64_t nh = (int64_t)T.halo.size();
+                const int64_t ne = (int64_t)(T.act.size() + T.rest.size());
+                for (auto *v : {&T.act, &T.rest}) P.ent_spring.insert(P.ent_spring.end(), v->begin(), v->end());
+                P.ent_ends.resize(P.ent_spring.size(), 0u);
+                P.halo.insert(P.halo.end(), T.halo.begin(), T.halo.end());
+                while (P.halo.size() % 4) P.halo.push_back(T.halo.empty() ? (int32_t)lo : T.halo.back());
+                P.tile_nh.push_back((int32_t)nh);
+                P.tile_nact.push_back((int32_t)T.act.size());
 
-            int nheavy = 0;
-            const int64_t nwarps = (nm + 31) / 32;
-            for (int64_t w = 0; w < nwarps; w++) {
-                int64_t m0 = lo + 32 * w, m1 = std::min(m0 + 32, hi);
-                int64_t width = 0;
-                for (int64_t m = m0; m < m1; m++) {
-                    int64_t d = ip[m + 1] - ip[m];
-                    if (d <= in.heavy_threshold) width = std::max(width, d);
-                }
-                width = (width + 3) & ~int64_t(3);
-                if (P.inc.size() > 0xffffffffULL - (uint64_t)(width * 32))
-                    return "incidence table exceeds 2^32 words";
-                P.warp_inc_off.push_back((uint32_t)P.inc.size());
-                // padding codes name slot ne, one past the tile's entries: a
-                // kernel that keeps a zero force there can sum whole words
-                P.inc.resize(P.inc.size() + (size_t)(width * 32), (uint16_t)ne);
-                for (int64_t m = m0; m < m1; m++) {
-                    int64_t d = ip[m + 1] - ip[m];
-                    if (d <= in.heavy_threshold) {
-                        P.deg[m] = (uint8_t)d;
-                    } else {
-                        P.deg[m] = 255;
-                        P.heavy_local.push_back((uint16_t)(m - lo));
-                        P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
-                        P.heavy_inc.resize(P.heavy_inc.size() + (size_t)d, 0);
-                        nheavy++;
+                int nheavy = 0;
+                const int64_t nwarps = (nm + 31) / 32;
+                for (int64_t w = 0; w < nwarps; w++) {
+                    int64_t m0 = lo + 32 * w, m1 = std::min(m0 + 32, hi);
+                    int64_t width = 0;
+                    for (int64_t m = m0; m < m1; m++) {
+                        int64_t d = ip[m + 1] - ip[m];
+                        if (d <= in.heavy_threshold) width = std::max(width, d);
+                    }
+                    width = (width + 3) & ~int64_t(3);
+                    if (P.inc.size() > 0xffffffffULL - (uint64_t)(width * 32))
+                        return "incidence table exceeds 2^32 words";
+                    P.warp_inc_off.push_back((uint32_t)P.inc.size());
+                    // padding codes name slot ne, one past the tile's entries: a
+                    // kernel that keeps a zero force there can sum whole words
+                    P.inc.resize(P.inc.size() + (size_t)(width * 32), (uint16_t)ne);
+                    for (int64_t m = m0; m < m1; m++) {
+                        int64_t d = ip[m + 1] - ip[m];
+                        if (d <= in.heavy_threshold) {
+                            P.deg[m] = (uint8_t)d;
+                        } else {
+                            P.deg[m] = 255;
+                            P.heavy_local.push_back((uint16_t)(m - lo));
+                            P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
+                            P.heavy_inc.resize(P.heavy_inc.size() + (size_t)d, 0);
+                            nheavy++;
+                        }
                     }
                 }
+                P.body_of_tile.push_back(leaf_body[f0 + i]);
+                P.tile_mass_off.push_back(hi);
+                P.tile_halo_off.push_back((int64_t)P.halo.size());
+                P.tile_ent_off.push_back((int64_t)P.ent_ends.size());
+                P.tile_warp_off.push_back(P.tile_warp_off.back() + nwarps);
+                P.tile_heavy_off.push_back((int64_t)P.heavy_local.size());
+                P.max_nm = std::max<int>(P.max_nm, (int)nm);
+                P.max_slots = std::max<int>(P.max_slots, (int)(nm + nh));
+                P.max_entries = std::max<int>(P.max_entries, (int)ne);
+                P.max_heavy = std::max(P.max_heavy, nheavy);
             }
-            P.body_of_tile.push_back((int32_t)b);
-            P.tile_mass_off.push_back(hi);
-            P.tile_halo_off.push_back((int64_t)P.halo.size());
-            P.tile_ent_off.push_back((int64_t)P.ent_ends.size());
-            P.tile_warp_off.push_back(P.tile_warp_off.back() + nwarps);
-            P.tile_heavy_off.push_back((int64_t)P.heavy_local.size());
-            P.max_nm = std::max<int>(P.max_nm, (int)nm);
-            P.max_slots = std::max<int>(P.max_slots, (int)(nm + nh));
-            P.max_entries = std::max<int>(P.max_entries, (int)ne);
-            P.max_heavy = std::max(P.max_heavy, nheavy);
         }
     }
     P.heavy_inc_off.push_back((uint32_t)P.heavy_inc.size());
@@ -566,20 +725,9 @@ std::string build_plan(const PlanInput &in, Plan &P) {
 
     // ---- slab order, entry words and incidence codes, tiles in parallel ---
     // (each tile writes only its own ranges of the tables)
-    {
-        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        const int nt = (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), std::max<int64_t>(1, P.ntiles / 8));
-        std::atomic<int64_t> next{0};
-        auto worker = [&]() {
-            PermuteScratch scratch;
-            for (int64_t t; (t = next.fetch_add(1)) < P.ntiles;)
-                order_tile(in, P, t, L, R, ip, isp, isg, scratch);
-        };
-        std::vector<std::thread> pool;
-        for (int q = 1; q < nt; q++) pool.emplace_back(worker);
-        worker();
-        for (auto &th : pool) th.join();
-    }
+    parallel_items<PermuteScratch>(P.ntiles, 8, [&](PermuteScratch &W, int64_t t) {
+        order_tile(in, P, t, L, R, ip, isp, isg, W);
+    });
     return "";
 }
 
