@@ -1,7 +1,10 @@
 """Host logic of the rollout server (titan_gb300/serving.py) on the CPU:
 admission by the HBM budget and by max_active, engine pooling per design,
-and complete per-request records.  The engine is a stand-in that finishes
-a rollout after a fixed number of polls; the GPU tests cover the real one."""
+complete per-request records, and planning of new designs on host threads.
+The engine is a stand-in that finishes a rollout after a fixed number of
+polls; the GPU tests cover the real one."""
+import time
+
 import numpy as np
 import pytest
 
@@ -122,3 +125,36 @@ def test_small_designs_are_planned_as_one_tile(fake):
     n7 = wl.rollout_request(7, 0)["pos"].shape[0]
     assert tiles[3] == 32 and tiles[7] == n7  # one resident tile each (at least 32 masses)
     assert tiles[12] == 128                    # larger: the per-tile kernel with 128-mass tiles
+
+
+class SlowPlanEngine(FakeEngine):
+    """Planning a design of side 12 takes 0.3 s; side 13 fails to plan."""
+
+    def plan_host(self, tile):
+        if self.n == wl.rollout_request(12, 0)["pos"].shape[0]:
+            time.sleep(0.3)
+        if self.n == wl.rollout_request(13, 0)["pos"].shape[0]:
+            raise RuntimeError("plan_host: planning failed")
+        super().plan_host(tile)
+
+
+def test_planning_a_new_design_does_not_hold_up_others(monkeypatch):
+    monkeypatch.setattr(serving, "Sim", SlowPlanEngine)
+    FakeEngine.live = FakeEngine.max_live = FakeEngine.built = 0
+    reqs = [{"id": 0, "arrival_s": 0.0, "side": 12, "steps": 100, "seed": 1}]
+    reqs += [{"id": i, "arrival_s": 0.001 * i, "side": 4, "steps": 100, "seed": i} for i in range(1, 6)]
+    recs, stats = serving.RolloutServer(hbm_budget_bytes=1e12).run(reqs)
+    assert stats["requests"] == 6
+    # the side-4 requests arrive later but finish while side 12 is still planning
+    assert max(recs[i]["done_s"] for i in range(1, 6)) < recs[0]["start_s"]
+    assert recs[0]["start_s"] >= 0.3
+
+
+def test_a_planning_error_reaches_the_caller(monkeypatch):
+    monkeypatch.setattr(serving, "Sim", SlowPlanEngine)
+    reqs = [{"id": 0, "arrival_s": 0.0, "side": 13, "steps": 100, "seed": 1},
+            {"id": 1, "arrival_s": 0.0, "side": 4, "steps": 100, "seed": 2}]
+    srv = serving.RolloutServer(hbm_budget_bytes=1e12)
+    with pytest.raises(RuntimeError, match="planning failed"):
+        srv.run(reqs)
+    assert not srv.planning and 13 not in srv.templates

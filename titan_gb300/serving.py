@@ -15,6 +15,10 @@ per process):
     state, spring parameters and clock (no reallocation, no replanning, the
     CUDA graphs stay cached), and the first engine of a design takes its
     plan from a host-planned template (adopt_plan);
+  * a new design is planned on a host thread (the planner is native code
+    and runs without the interpreter lock), so rollouts of planned designs
+    keep being admitted and polled meanwhile; among arrived requests, those
+    whose design is planned start in arrival order;
   * a design small enough for one CTA's shared memory runs as one tile of
     its own size: a halo-free tile, stepped for the whole rollout by one
     resident-tile launch (one CTA, no per-step launches);
@@ -25,6 +29,7 @@ from __future__ import annotations
 
 import collections
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -60,6 +65,8 @@ class RolloutServer:
         self.max_active = max_active
         self.pool_per_design = pool_per_design
         self.templates = {}                          # side -> planned host-only Sim
+        self.planning = {}                           # side -> (host-only Sim, Future of its plan)
+        self._planner = None                         # host threads for planning, during run()
         self.pool = collections.defaultdict(list)    # side -> idle started engines
         self.bytes_of = {}                           # side -> device bytes of one engine
         self.used = 0.0
@@ -72,8 +79,51 @@ class RolloutServer:
         n, ns = sc["pos"].shape[0], sc["left"].size
         return 400.0 * n + 96.0 * ns + (8 << 20)
 
+    def _choice(self, n, ns):
+        """(kernel, tile) for a design of n masses and ns springs."""
+        if self.resident_tiles and resident_tile_fits(self.precision, n, ns):
+            return 0, max(32, n)  # one halo-free tile: a resident-tile launch per rollout
+        if n < self.small_masses:
+            return 1, 128
+        return 0, 0
+
+    def _template(self, side, sc):
+        """A host-only handle of design `side`, loaded (not yet planned)."""
+        kernel, _ = self._choice(sc["pos"].shape[0], sc["left"].size)
+        t = Sim(self.precision, self.device)
+        wl.load(t, sc, start=False, kernel=kernel)
+        return t
+
+    def _plan_async(self, side, sc):
+        """Start planning design `side` on a host thread (once)."""
+        if side in self.templates or side in self.planning:
+            return
+        t = self._template(side, sc)
+        _, tile = self._choice(sc["pos"].shape[0], sc["left"].size)
+        if self._planner is None:
+            self._planner = ThreadPoolExecutor(max_workers=2, thread_name_prefix="titan-plan")
+        self.planning[side] = (t, self._planner.submit(t.plan_host, tile))
+
+    def _collect_plans(self):
+        """Move finished plans to the templates; a planning error is raised
+        here.  Returns whether one finished."""
+        done = [side for side, (_, f) in self.planning.items() if f.done()]
+        for side in done:
+            t, f = self.planning.pop(side)
+            try:
+                f.result()
+            except BaseException:
+                t.close()
+                raise
+            self.templates[side] = t
+        return bool(done)
+
+    def _planned(self, side):
+        return side in self.templates or bool(self.pool[side])
+
     def _engine(self, side, sc):
-        """An engine loaded with scene sc, ready at time 0."""
+        """An engine loaded with scene sc, ready at time 0 (planning the
+        design here if no template exists yet)."""
         if self.pool[side]:
             e = self.pool[side].pop()
             n = e.n
@@ -82,16 +132,9 @@ class RolloutServer:
                                 omega=sc["omega"], amp=sc["amp"], phase=sc["phase"])
             e.set_time(0.0)
             return e
-        n, ns = sc["pos"].shape[0], sc["left"].size
-        if self.resident_tiles and resident_tile_fits(self.precision, n, ns):
-            kernel, tile = 0, max(32, n)  # one halo-free tile: a resident-tile launch per rollout
-        elif n < self.small_masses:
-            kernel, tile = 1, 128
-        else:
-            kernel, tile = 0, 0
+        kernel, tile = self._choice(sc["pos"].shape[0], sc["left"].size)
         if side not in self.templates:
-            t = Sim(self.precision, self.device)
-            wl.load(t, sc, start=False, kernel=kernel)
+            t = self._template(side, sc)
             t.plan_host(tile)
             self.templates[side] = t
         e = Sim(self.precision, self.device)
@@ -116,51 +159,86 @@ class RolloutServer:
         Returns per-request records and summary statistics."""
         scene_of = scene_of or (lambda r: wl.rollout_request(r["side"], r["seed"]))
         pending = collections.deque(sorted(requests, key=lambda r: r["arrival_s"]))
+        scenes = {}  # id -> scene, built once per arrived request
         active = []
         records = {}
         springs_done = 0
         t0 = time.perf_counter()
-        while pending or active:
-            now = time.perf_counter() - t0
-            progressed = False
-            while pending and pending[0]["arrival_s"] * time_scale <= now and len(active) < self.max_active:
-                r = pending[0]
-                sc = scene_of(r)
-                need = self._estimate(r["side"], sc)
-                if active and self.used + need > self.budget:
-                    break  # admission by HBM budget: wait for a rollout to finish
-                pending.popleft()
-                e = self._engine(r["side"], sc)
-                e.step(r["steps"])
-                self.used += need
-                active.append((r, e, need, time.perf_counter() - t0, sc["left"].size))
-                progressed = True
-            still = []
-            for r, e, need, started, ns in active:
-                if e.poll():
-                    pos = e.get_state(pos=True, vel=False)["pos"]
-                    done = time.perf_counter() - t0
-                    rec = {"id": r["id"], "arrival_s": r["arrival_s"] * time_scale, "start_s": started,
-                           "done_s": done, "latency_ms": (done - r["arrival_s"] * time_scale) * 1e3,
-                           "steps": r["steps"], "masses": pos.shape[0], "springs": ns}
-                    if keep_results:
-                        rec["pos"] = pos
-                    records[r["id"]] = rec
-                    springs_done += ns * r["steps"]
-                    self.used -= need
-                    self._release(r["side"], e)
+        try:
+            while pending or active:
+                now = time.perf_counter() - t0
+                # plans of new designs finish on host threads
+                progressed = self._collect_plans()
+                idx = 0
+                while idx < len(pending) and len(active) < self.max_active:
+                    r = pending[idx]
+                    if r["arrival_s"] * time_scale > now:
+                        break
+                    if r["id"] not in scenes:
+                        scenes[r["id"]] = scene_of(r)
+                    sc = scenes[r["id"]]
+                    if not self._planned(r["side"]):
+                        self._plan_async(r["side"], sc)  # admitted once its design is planned
+                        idx += 1
+                        continue
+                    need = self._estimate(r["side"], sc)
+                    if active and self.used + need > self.budget:
+                        break  # admission by HBM budget: wait for a rollout to finish
+                    del pending[idx]
+                    del scenes[r["id"]]
+                    e = self._engine(r["side"], sc)
+                    e.step(r["steps"])
+                    self.used += need
+                    active.append((r, e, need, time.perf_counter() - t0, sc["left"].size))
                     progressed = True
-                else:
-                    still.append((r, e, need, started, ns))
-            active = still
-            if not progressed:
-                time.sleep(50e-6)
+                finished, springs = self._poll(active, records, keep_results, t0, time_scale)
+                springs_done += springs
+                if not (progressed or finished):
+                    time.sleep(50e-6)
+        finally:
+            if self._planner is not None:
+                self._planner.shutdown(wait=True)
+                self._planner = None
+            self._collect_finished_quietly()
         wall = time.perf_counter() - t0
         lat = np.array([rec["latency_ms"] for rec in records.values()])
         stats = {"requests": len(records), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
                  "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
                  "spring_updates_per_s": springs_done / wall, "engines_built": self.engines_built}
         return records, stats
+
+    def _collect_finished_quietly(self):
+        """After run(): keep finished plans as templates, drop failed ones."""
+        for side, (t, f) in list(self.planning.items()):
+            if f.done() and f.exception() is None:
+                self.templates[side] = t
+            else:
+                t.close()
+        self.planning.clear()
+
+    def _poll(self, active, records, keep_results, t0, time_scale):
+        """Retire finished rollouts from `active` (in place) into records.
+        Returns (whether one finished, their spring updates)."""
+        still = []
+        finished, springs = False, 0
+        for r, e, need, started, ns in active:
+            if not e.poll():
+                still.append((r, e, need, started, ns))
+                continue
+            pos = e.get_state(pos=True, vel=False)["pos"]
+            done = time.perf_counter() - t0
+            rec = {"id": r["id"], "arrival_s": r["arrival_s"] * time_scale, "start_s": started,
+                   "done_s": done, "latency_ms": (done - r["arrival_s"] * time_scale) * 1e3,
+                   "steps": r["steps"], "masses": pos.shape[0], "springs": ns}
+            if keep_results:
+                rec["pos"] = pos
+            records[r["id"]] = rec
+            springs += ns * r["steps"]
+            self.used -= need
+            self._release(r["side"], e)
+            finished = True
+        active[:] = still
+        return finished, springs
 
     def close(self):
         for lst in self.pool.values():
