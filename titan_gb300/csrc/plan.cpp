@@ -31,8 +31,10 @@ uint64_t spread21(uint64_t v) {
 // and its end (offset base + position) is appended to leaf_end.  Ties on
 // the split axis are broken by Morton code, then index: a total order, so
 // the leaves' contents do not depend on the selection algorithm.
+// The two halves of a cut are independent: down to `par_depth` levels the
+// second half runs on its own thread, its leaves appended after the first's.
 void bisect(int32_t *ids, int64_t cnt, int cap, const std::vector<uint32_t> &qc, const std::vector<uint64_t> &code,
-            int64_t base, std::vector<int64_t> &leaf_end) {
+            int64_t base, std::vector<int64_t> &leaf_end, int par_depth = 0) {
     if (cnt <= 0) return;
     const int64_t m = (cnt + cap - 1) / cap;
     if (m <= 1) {
@@ -55,6 +57,14 @@ void bisect(int32_t *ids, int64_t cnt, int cap, const std::vector<uint32_t> &qc,
         const uint32_t xa = qc[3 * (size_t)a + ax], xc = qc[3 * (size_t)c + ax];
         return xa < xc || (xa == xc && (code[a] < code[c] || (code[a] == code[c] && a < c)));
     });
+    if (par_depth > 0 && cnt >= (int64_t)1 << 15) {
+        std::vector<int64_t> second;
+        std::thread th([&] { bisect(ids + k, cnt - k, cap, qc, code, base + k, second, par_depth - 1); });
+        bisect(ids, k, cap, qc, code, base, leaf_end, par_depth - 1);
+        th.join();
+        leaf_end.insert(leaf_end.end(), second.begin(), second.end());
+        return;
+    }
     bisect(ids, k, cap, qc, code, base, leaf_end);
     bisect(ids + k, cnt - k, cap, qc, code, base + k, leaf_end);
 }
@@ -386,6 +396,8 @@ void parallel_items(int64_t count, int64_t grain, F &&f) {
     for (auto &th : pool) th.join();
 }
 
+struct NoScratch {};
+
 // One tile of the layout: masses [lo, hi); its slab entries (every spring
 // that a free mass of the tile is an end of, once) in ascending spring
 // order, actuated ones apart; the other ends outside the tile (its halo),
@@ -570,7 +582,10 @@ std::string build_plan(const PlanInput &in, Plan &P) {
     std::vector<uint64_t> code(n, 0);
     std::vector<uint32_t> qc(3 * (size_t)n, 0);
     std::vector<int64_t> leaf_end;  // new-index end of each leaf, in order
-    for (int64_t b = 0; b < P.nbodies; b++) {
+    // bodies on several threads (each writes only its own ranges); a lone
+    // body cuts its top levels on several threads instead
+    std::vector<std::vector<int64_t>> body_leaves((size_t)P.nbodies);
+    parallel_items<NoScratch>(P.nbodies, 16, [&](NoScratch &, int64_t b) {
         int64_t b0 = bptr[b], b1 = bptr[b + 1];
         double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         for (int64_t i = b0; i < b1; i++)
@@ -597,40 +612,82 @@ std::string build_plan(const PlanInput &in, Plan &P) {
             code[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
         }
         const int cap_b = (b1 - b0) <= (int64_t)in.whole_cap ? (int)(b1 - b0) : in.tile_cap;
-        bisect(P.new2old.data() + b0, b1 - b0, cap_b, qc, code, b0, leaf_end);
-    }
+        bisect(P.new2old.data() + b0, b1 - b0, cap_b, qc, code, b0, body_leaves[b], P.nbodies == 1 ? 4 : 0);
+    });
+    for (const auto &v : body_leaves) leaf_end.insert(leaf_end.end(), v.begin(), v.end());
     P.old2new.resize(n);
     for (int64_t i = 0; i < n; i++) P.old2new[P.new2old[i]] = (int32_t)i;
 
     // ---- springs in the new numbering -----------------------------------
+    // (chunks of springs on several threads)
+    constexpr int64_t kChunk = 1 << 16;
+    const int64_t nchunks = (ns + kChunk - 1) / kChunk;
     std::vector<int32_t> L(ns, -1), R(ns, -1);
-    for (int64_t s = 0; s < ns; s++) {
-        int32_t l = in.left[s], r = in.right[s];
-        if (l < 0 || r < 0 || l >= n || r >= n) continue;  // skipped as src/sim.cu:1052 does
-        L[s] = P.old2new[l];
-        R[s] = P.old2new[r];
-        P.valid_springs++;
-    }
-    auto is_fixed_new = [&](int64_t m) { return in.fixed && in.fixed[P.new2old[m]]; };
+    std::vector<int64_t> chunk_valid((size_t)nchunks, 0);
+    parallel_items<NoScratch>(nchunks, 4, [&](NoScratch &, int64_t c) {
+        for (int64_t s = c * kChunk; s < std::min(ns, (c + 1) * kChunk); s++) {
+            int32_t l = in.left[s], r = in.right[s];
+            if (l < 0 || r < 0 || l >= n || r >= n) continue;  // skipped as src/sim.cu:1052 does
+            L[s] = P.old2new[l];
+            R[s] = P.old2new[r];
+            chunk_valid[c]++;
+        }
+    });
+    for (int64_t v : chunk_valid) P.valid_springs += v;
+    std::vector<uint8_t> fixed_new(n, 0);
+    if (in.fixed)
+        for (int64_t m = 0; m < n; m++) fixed_new[m] = in.fixed[P.new2old[m]] ? 1 : 0;
 
     // incidence of each (non-fixed) mass, ascending spring order; for a spring
-    // attached twice to one mass the right end comes first (src/sim.cu:1067-1077)
+    // attached twice to one mass the right end comes first (src/sim.cu:1067-1077).
+    // Counted and filled on several threads, then each mass's list sorted.
+    std::vector<std::atomic<int64_t>> fillc((size_t)n);  // value-initialised: zero
+    parallel_items<NoScratch>(nchunks, 4, [&](NoScratch &, int64_t c) {
+        for (int64_t s = c * kChunk; s < std::min(ns, (c + 1) * kChunk); s++) {
+            if (L[s] < 0) continue;
+            if (!fixed_new[R[s]]) fillc[R[s]].fetch_add(1, std::memory_order_relaxed);
+            if (!fixed_new[L[s]]) fillc[L[s]].fetch_add(1, std::memory_order_relaxed);
+        }
+    });
     std::vector<int64_t> ip(n + 1, 0);
-    for (int64_t s = 0; s < ns; s++) {
-        if (L[s] < 0) continue;
-        if (!is_fixed_new(R[s])) ip[R[s] + 1]++;
-        if (!is_fixed_new(L[s])) ip[L[s] + 1]++;
+    for (int64_t i = 0; i < n; i++) {
+        ip[i + 1] = ip[i] + fillc[i].load(std::memory_order_relaxed);
+        fillc[i].store(ip[i], std::memory_order_relaxed);
     }
-    for (int64_t i = 0; i < n; i++) ip[i + 1] += ip[i];
     std::vector<int64_t> isp(ip[n]);
     std::vector<int8_t> isg(ip[n]);
-    {
-        std::vector<int64_t> fill(ip.begin(), ip.end() - 1);
-        for (int64_t s = 0; s < ns; s++) {
+    parallel_items<NoScratch>(nchunks, 4, [&](NoScratch &, int64_t c) {
+        for (int64_t s = c * kChunk; s < std::min(ns, (c + 1) * kChunk); s++) {
             if (L[s] < 0) continue;
-            if (!is_fixed_new(R[s])) { isp[fill[R[s]]] = s; isg[fill[R[s]]] = 1; fill[R[s]]++; }
-            if (!is_fixed_new(L[s])) { isp[fill[L[s]]] = s; isg[fill[L[s]]] = -1; fill[L[s]]++; }
+            if (!fixed_new[R[s]]) {
+                const int64_t q = fillc[R[s]].fetch_add(1, std::memory_order_relaxed);
+                isp[q] = s;
+                isg[q] = 1;
+            }
+            if (!fixed_new[L[s]]) {
+                const int64_t q = fillc[L[s]].fetch_add(1, std::memory_order_relaxed);
+                isp[q] = s;
+                isg[q] = -1;
+            }
         }
+    });
+    {
+        constexpr int64_t kMassChunk = 1 << 14;
+        parallel_items<NoScratch>((n + kMassChunk - 1) / kMassChunk, 4, [&](NoScratch &, int64_t c) {
+            std::vector<std::pair<int64_t, int8_t>> v;
+            for (int64_t m = c * kMassChunk; m < std::min(n, (c + 1) * kMassChunk); m++) {
+                v.clear();
+                for (int64_t q = ip[m]; q < ip[m + 1]; q++) v.emplace_back(isp[q], isg[q]);
+                // ascending spring; right end (+1) before left end (-1)
+                std::sort(v.begin(), v.end(), [](const auto &a, const auto &b) {
+                    return a.first < b.first || (a.first == b.first && a.second > b.second);
+                });
+                for (int64_t q = ip[m]; q < ip[m + 1]; q++) {
+                    isp[q] = v[q - ip[m]].first;
+                    isg[q] = v[q - ip[m]].second;
+                }
+            }
+        });
     }
 
     // ---- tiles ------------------------------------------------------------
