@@ -346,10 +346,14 @@ int titan_gb300_plan_info(const titan_gb300_sim *sim, int64_t out[12]);
 
 /* ---- host-only helpers (no GPU needed) ------------------------------------ */
 
-/* Builds the tile plan of the current scene on the host only (no CUDA call),
- * for inspection and validation; start() builds its own.  The tables are
- * copied out with titan_gb300_plan_table, which returns the element count
- * (and copies when out != NULL), or -1 for an unknown table. */
+/* Builds the tile plan of the current scene on the host only (no GPU work;
+ * with tile_masses 0 the default tile reads the device's SM count, 152 when
+ * there is no device), for inspection, validation and adopt_plan; start()
+ * builds its own otherwise.  The planner runs on up to 16 host threads
+ * (environment variable TITAN_GB300_PLAN_THREADS: another limit, 1 to 64);
+ * the plan is the same for any thread count.  The tables are copied out
+ * with titan_gb300_plan_table, which returns the element count (and copies
+ * when out != NULL), or -1 for an unknown table. */
 int titan_gb300_plan_host(titan_gb300_sim *sim, int tile_masses);
 int64_t titan_gb300_plan_table(const titan_gb300_sim *sim, int table, void *out);
 #define TITAN_GB300_T_NEW2OLD 0        /* int32: tiled index -> creation index   */

@@ -492,3 +492,16 @@ def test_set_integrator_validates():
     s.set_integrator(tg.RK2)
     s.set_integrator(tg.VERLET)
     s.close()
+
+
+def test_plan_does_not_depend_on_planner_threads(monkeypatch):
+    """Every planner pass splits its work over host threads; one thread and
+    many give the same tables (a lone body and a batch of bodies)."""
+    scenes = [(wl.actuated_lattice(n_side=40), 0), (wl.robot_batch(nbodies=96, seed=2, side_range=(3, 10)), 0)]
+    for sc, tile in scenes:
+        monkeypatch.setenv("TITAN_GB300_PLAN_THREADS", "1")
+        one = plan_tables(sc, tile)
+        monkeypatch.setenv("TITAN_GB300_PLAN_THREADS", "13")
+        many = plan_tables(sc, tile)
+        for k in one:
+            assert np.array_equal(one[k], many[k]), k

@@ -5,6 +5,7 @@
 #include <thread>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -31,6 +32,16 @@ uint64_t spread21(uint64_t v) {
 // and its end (offset base + position) is appended to leaf_end.  Ties on
 // the split axis are broken by Morton code, then index: a total order, so
 // the leaves' contents do not depend on the selection algorithm.
+// Host threads of the planner: TITAN_GB300_PLAN_THREADS when set (1 to
+// 64), else the host's processors, at most 16.  The plan does not depend on it.
+int planner_threads() {
+    if (const char *e = std::getenv("TITAN_GB300_PLAN_THREADS")) {
+        const int v = std::atoi(e);
+        if (v >= 1) return std::min(v, 64);
+    }
+    return (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+}
+
 // The two halves of a cut are independent: down to `par_depth` levels the
 // second half runs on its own thread, its leaves appended after the first's.
 void bisect(int32_t *ids, int64_t cnt, int cap, const std::vector<uint32_t> &qc, const std::vector<uint64_t> &code,
@@ -378,13 +389,12 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
     for (int64_t p = 0; p < ne; p++) (p < na ? act[p] : rest[p - na]) = seq[at[p]];
 }
 
-// Runs f(state, i) for every i in [0, count) on up to 16 host threads, each
-// with its own State; at least `grain` items per thread.  f may write only
-// what belongs to item i.
+// Runs f(state, i) for every i in [0, count) on up to planner_threads()
+// host threads, each with its own State; at least `grain` items per thread.
+// f may write only what belongs to item i.
 template <class State, class F>
 void parallel_items(int64_t count, int64_t grain, F &&f) {
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int nt = (int)std::min<int64_t>(std::min<unsigned>(hw, 16u), std::max<int64_t>(1, count / grain));
+    const int nt = (int)std::min<int64_t>(planner_threads(), std::max<int64_t>(1, count / grain));
     std::atomic<int64_t> next{0};
     auto worker = [&]() {
         State state;
@@ -612,7 +622,9 @@ std::string build_plan(const PlanInput &in, Plan &P) {
             code[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
         }
         const int cap_b = (b1 - b0) <= (int64_t)in.whole_cap ? (int)(b1 - b0) : in.tile_cap;
-        bisect(P.new2old.data() + b0, b1 - b0, cap_b, qc, code, b0, body_leaves[b], P.nbodies == 1 ? 4 : 0);
+        int depth = 0;  // a lone body: about one cut's half per thread
+        while (P.nbodies == 1 && (2 << depth) <= planner_threads() && depth < 6) depth++;
+        bisect(P.new2old.data() + b0, b1 - b0, cap_b, qc, code, b0, body_leaves[b], depth);
     });
     for (const auto &v : body_leaves) leaf_end.insert(leaf_end.end(), v.begin(), v.end());
     P.old2new.resize(n);
