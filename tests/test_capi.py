@@ -505,3 +505,32 @@ def test_plan_does_not_depend_on_planner_threads(monkeypatch):
         many = plan_tables(sc, tile)
         for k in one:
             assert np.array_equal(one[k], many[k]), k
+
+
+CHILD_OOM = r"""
+import resource, sys
+sys.path.insert(0, sys.argv[1])
+import titan_gb300 as tg
+from titan_gb300 import workloads as wl
+s = tg.Sim(tg.FP32C)
+wl.load(s, wl.actuated_lattice(n_side=60), start=False)
+vm = next(int(l.split()[1]) for l in open("/proc/self/status") if l.startswith("VmSize:")) * 1024
+resource.setrlimit(resource.RLIMIT_AS, (vm + (64 << 20), resource.getrlimit(resource.RLIMIT_AS)[1]))
+try:
+    s.plan_host(208)
+    print("PLANNED")
+except tg.TitanError as e:
+    print("ERROR", e)
+"""
+
+
+def test_planner_out_of_host_memory_is_an_error_code():
+    """The planner's threads hand an allocation failure back to the caller:
+    plan_host returns an error (no abort) when host memory runs out."""
+    import subprocess
+    import sys
+    if not Path("/proc/self/status").exists():
+        pytest.skip("needs /proc")
+    r = subprocess.run([sys.executable, "-c", CHILD_OOM, str(ROOT)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "ERROR" in r.stdout and ("memory" in r.stdout or "planning failed" in r.stdout), r.stdout

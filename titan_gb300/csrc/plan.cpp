@@ -2,6 +2,7 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <system_error>
 #include <thread>
 #include <atomic>
 #include <cmath>
@@ -9,6 +10,9 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <new>
+#include <mutex>
+#include <exception>
 #include <numeric>
 #include <utility>
 
@@ -70,9 +74,29 @@ void bisect(int32_t *ids, int64_t cnt, int cap, const std::vector<uint32_t> &qc,
     });
     if (par_depth > 0 && cnt >= (int64_t)1 << 15) {
         std::vector<int64_t> second;
-        std::thread th([&] { bisect(ids + k, cnt - k, cap, qc, code, base + k, second, par_depth - 1); });
-        bisect(ids, k, cap, qc, code, base, leaf_end, par_depth - 1);
+        std::exception_ptr err;
+        std::thread th;
+        try {
+            th = std::thread([&] {
+                try {
+                    bisect(ids + k, cnt - k, cap, qc, code, base + k, second, par_depth - 1);
+                } catch (...) {
+                    err = std::current_exception();
+                }
+            });
+        } catch (const std::system_error &) {  // no thread to be had: both halves here
+            bisect(ids, k, cap, qc, code, base, leaf_end, par_depth - 1);
+            bisect(ids + k, cnt - k, cap, qc, code, base + k, leaf_end, par_depth - 1);
+            return;
+        }
+        try {
+            bisect(ids, k, cap, qc, code, base, leaf_end, par_depth - 1);
+        } catch (...) {
+            th.join();
+            throw;
+        }
         th.join();
+        if (err) std::rethrow_exception(err);
         leaf_end.insert(leaf_end.end(), second.begin(), second.end());
         return;
     }
@@ -392,18 +416,35 @@ void gather_permute(std::vector<int64_t> &act, std::vector<int64_t> &rest, int64
 // Runs f(state, i) for every i in [0, count) on up to planner_threads()
 // host threads, each with its own State; at least `grain` items per thread.
 // f may write only what belongs to item i.
+// An exception in any thread stops the others taking items and is rethrown
+// here once all have joined.
 template <class State, class F>
 void parallel_items(int64_t count, int64_t grain, F &&f) {
     const int nt = (int)std::min<int64_t>(planner_threads(), std::max<int64_t>(1, count / grain));
     std::atomic<int64_t> next{0};
+    std::exception_ptr err;
+    std::mutex err_mu;
     auto worker = [&]() {
-        State state;
-        for (int64_t i; (i = next.fetch_add(1)) < count;) f(state, i);
+        try {
+            State state;
+            for (int64_t i; (i = next.fetch_add(1)) < count;) f(state, i);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(err_mu);
+            if (!err) err = std::current_exception();
+            next.store(count);
+        }
     };
     std::vector<std::thread> pool;
-    for (int q = 1; q < nt; q++) pool.emplace_back(worker);
+    for (int q = 1; q < nt; q++) {
+        try {
+            pool.emplace_back(worker);
+        } catch (const std::system_error &) {
+            break;  // no thread to be had: fewer threads take the items
+        }
+    }
     worker();
     for (auto &th : pool) th.join();
+    if (err) std::rethrow_exception(err);
 }
 
 struct NoScratch {};
@@ -555,7 +596,7 @@ void order_tile(const PlanInput &in, Plan &P, int64_t t, const std::vector<int32
 
 }  // namespace
 
-std::string build_plan(const PlanInput &in, Plan &P) {
+static std::string build_plan_tables(const PlanInput &in, Plan &P) {
     P = Plan();
     const int64_t n = in.n, ns = in.ns;
     P.n = n;
@@ -798,6 +839,18 @@ std::string build_plan(const PlanInput &in, Plan &P) {
         order_tile(in, P, t, L, R, ip, isp, isg, W);
     });
     return "";
+}
+
+std::string build_plan(const PlanInput &in, Plan &P) {
+    try {
+        return build_plan_tables(in, P);
+    } catch (const std::bad_alloc &) {
+        P = Plan();
+        return "host memory exhausted while planning";
+    } catch (const std::exception &e) {
+        P = Plan();
+        return std::string("planning failed: ") + e.what();
+    }
 }
 
 void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_cap, ResPlan &R) {

@@ -75,7 +75,7 @@ struct Plan {
 };
 
 // Returns "" on success, otherwise the reason (e.g. a mass whose degree does
-// not fit one tile's slab).
+// not fit one tile's slab, or host memory exhausted); throws nothing.
 std::string build_plan(const PlanInput &in, Plan &out);
 
 // Body-resident plan: bodies small enough for one CTA keep their state in
