@@ -509,28 +509,43 @@ def test_plan_does_not_depend_on_planner_threads(monkeypatch):
 
 CHILD_OOM = r"""
 import resource, sys
+import numpy as np
 sys.path.insert(0, sys.argv[1])
 import titan_gb300 as tg
 from titan_gb300 import workloads as wl
+
+def limit_to_now_plus(extra):
+    vm = next(int(l.split()[1]) for l in open("/proc/self/status") if l.startswith("VmSize:")) * 1024
+    resource.setrlimit(resource.RLIMIT_AS, (vm + extra, resource.getrlimit(resource.RLIMIT_AS)[1]))
+
 s = tg.Sim(tg.FP32C)
-wl.load(s, wl.actuated_lattice(n_side=60), start=False)
-vm = next(int(l.split()[1]) for l in open("/proc/self/status") if l.startswith("VmSize:")) * 1024
-resource.setrlimit(resource.RLIMIT_AS, (vm + (64 << 20), resource.getrlimit(resource.RLIMIT_AS)[1]))
+if sys.argv[2] == "plan":
+    wl.load(s, wl.actuated_lattice(n_side=60), start=False)
+    limit_to_now_plus(64 << 20)
+    call = lambda: s.plan_host(208)
+else:  # host copies of 4M masses: pos and vel alone are 192 MB
+    n = 4 << 20
+    pos, vel, m = np.zeros((n, 3)), np.zeros((n, 3)), np.full(n, 0.1)
+    limit_to_now_plus(64 << 20)
+    call = lambda: s.set_masses(pos, m, vel=vel)
 try:
-    s.plan_host(208)
-    print("PLANNED")
+    call()
+    print("DONE")
 except tg.TitanError as e:
-    print("ERROR", e)
+    print("ERROR", e.code, e)
 """
 
 
-def test_planner_out_of_host_memory_is_an_error_code():
-    """The planner's threads hand an allocation failure back to the caller:
-    plan_host returns an error (no abort) when host memory runs out."""
+@pytest.mark.parametrize("what", ["plan", "masses"])
+def test_out_of_host_memory_is_an_error_code(what):
+    """A host allocation that fails inside an entry point (the planner's
+    threads included) comes back as a status, not an abort: the C ABI
+    throws nothing."""
     import subprocess
     import sys
     if not Path("/proc/self/status").exists():
         pytest.skip("needs /proc")
-    r = subprocess.run([sys.executable, "-c", CHILD_OOM, str(ROOT)], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([sys.executable, "-c", CHILD_OOM, str(ROOT), what], capture_output=True, text=True,
+                       timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
-    assert "ERROR" in r.stdout and ("memory" in r.stdout or "planning failed" in r.stdout), r.stdout
+    assert r.stdout.startswith("ERROR") and "memory" in r.stdout, r.stdout

@@ -996,11 +996,38 @@ int check_kernel_error(titan_gb300_sim *s) {
 
 }  // namespace
 
+// Status of a C++ exception that reached an entry point (a host allocation
+// that failed, or a library error): the C ABI throws nothing, and the
+// message goes to the handle when there is one.
+static int host_exception(titan_gb300_sim *s) noexcept {
+    int code = TITAN_GB300_EINVAL;
+    std::string msg = "host error";
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        code = TITAN_GB300_ENOMEM;
+        msg = "host memory exhausted";
+    } catch (const std::exception &e) {
+        try {
+            msg = std::string("host error: ") + e.what();
+        } catch (...) {
+        }
+    } catch (...) {
+    }
+    if (s) {
+        try {
+            s->err = msg;
+        } catch (...) {
+        }
+    }
+    return code;
+}
+
 extern "C" {
 
 const char *titan_gb300_version(void) { return "titan_gb300 0.1 (sm_103a)"; }
 
-int titan_gb300_create(titan_gb300_sim **out, int device, int precision) {
+int titan_gb300_create(titan_gb300_sim **out, int device, int precision) try {
     if (!out) return TITAN_GB300_EINVAL;
     *out = nullptr;
     if (precision < 0 || precision > 2 || device < 0) return TITAN_GB300_EINVAL;
@@ -1012,6 +1039,8 @@ int titan_gb300_create(titan_gb300_sim **out, int device, int precision) {
     s->prec = precision;
     *out = s;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(nullptr);
 }
 
 void titan_gb300_destroy(titan_gb300_sim *s) {
@@ -1020,30 +1049,36 @@ void titan_gb300_destroy(titan_gb300_sim *s) {
     delete s;
 }
 
-int titan_gb300_set_launch(titan_gb300_sim *s, int threads_per_cta) {
+int titan_gb300_set_launch(titan_gb300_sim *s, int threads_per_cta) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (threads_per_cta != 0 && (threads_per_cta < 64 || threads_per_cta > 512 || threads_per_cta % 32))
         return s->fail(TITAN_GB300_EINVAL, "threads per CTA must be 0 or a multiple of 32 in [64, 512]");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set the launch shape before start");
     s->threads_req = threads_per_cta;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_set_occupancy(titan_gb300_sim *s, int min_ctas_per_sm) {
+int titan_gb300_set_occupancy(titan_gb300_sim *s, int min_ctas_per_sm) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (min_ctas_per_sm < 0 || min_ctas_per_sm > 4 || min_ctas_per_sm == 2)
         return s->fail(TITAN_GB300_EINVAL, "minimum CTAs per SM must be 0, 1, 3 or 4");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set the occupancy before start");
     s->min_ctas_req = min_ctas_per_sm;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) {
+int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (variant < 0 || variant > 4) return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0 to 4");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "choose the kernel before start");
     s->kernel_req = variant;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
@@ -1062,7 +1097,7 @@ int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
     return TITAN_GB300_OK;
 }
 
-int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int threads_per_cta) {
+int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int threads_per_cta) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (mode < -1 || mode > 2) return s->fail(TITAN_GB300_EINVAL, "resident mode must be -1, 0, 1 or 2");
     if (bin_masses < 0 || bin_masses > 32767) return s->fail(TITAN_GB300_EINVAL, "bin size must be in [0, 32767]");
@@ -1073,6 +1108,8 @@ int titan_gb300_set_resident(titan_gb300_sim *s, int mode, int bin_masses, int t
     s->res_bin_req = bin_masses;
     s->res_threads_req = threads_per_cta;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_resident_info(const titan_gb300_sim *s, int64_t out[8]) {
@@ -1109,7 +1146,7 @@ int titan_gb300_resident_info(const titan_gb300_sim *s, int64_t out[8]) {
     return TITAN_GB300_OK;
 }
 
-int titan_gb300_adopt_plan(titan_gb300_sim *s, const titan_gb300_sim *src) {
+int titan_gb300_adopt_plan(titan_gb300_sim *s, const titan_gb300_sim *src) try {
     if (!s || !src) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "adopt a plan before start");
     if (src->plan.ntiles <= 0) return s->fail(TITAN_GB300_EINVAL, "the source handle has no plan");
@@ -1128,9 +1165,11 @@ int titan_gb300_adopt_plan(titan_gb300_sim *s, const titan_gb300_sim *src) {
     s->plan_req = src->plan_req;
     s->plan_adopted = true;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
+int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "plan_host is for scenes that have not started");
     if (s->n <= 0) return s->fail(TITAN_GB300_EINVAL, "no masses");
@@ -1143,6 +1182,8 @@ int titan_gb300_plan_host(titan_gb300_sim *s, int tile_masses) {
     const int cap = resident_cap(s);
     if (cap > 0) tg::build_resident(in, s->plan, cap, cap, s->rplan);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int64_t titan_gb300_plan_table(const titan_gb300_sim *s, int table, void *out) {
@@ -1190,7 +1231,7 @@ const char *titan_gb300_last_error(const titan_gb300_sim *s) {
 }
 
 int titan_gb300_set_masses(titan_gb300_sim *s, int64_t n, const double *pos, const double *vel,
-                           const double *m, const double *ext, const uint8_t *fixed, const double *drag) {
+                           const double *m, const double *ext, const uint8_t *fixed, const double *drag) try {
     if (!s) return TITAN_GB300_EINVAL;
     s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "masses can only be replaced before start");
@@ -1213,12 +1254,14 @@ int titan_gb300_set_masses(titan_gb300_sim *s, int64_t n, const double *pos, con
     s->lc_type.clear();
     s->lc_rec.clear();
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_set_springs(titan_gb300_sim *s, int64_t n, const int32_t *left, const int32_t *right,
                             const double *k, const double *rest, const double *damping,
                             const int32_t *type, const double *omega, const double *amp,
-                            const double *phase) {
+                            const double *phase) try {
     if (!s) return TITAN_GB300_EINVAL;
     s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "springs can only be replaced before start");
@@ -1243,10 +1286,12 @@ int titan_gb300_set_springs(titan_gb300_sim *s, int64_t n, const int32_t *left, 
     s->phase.clear();
     if (phase) s->phase.assign(phase, phase + n);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_set_local_constraints(titan_gb300_sim *s, const int64_t *mass_ptr, const int32_t *type,
-                                      const double *vec, const double *num) {
+                                      const double *vec, const double *num) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set local constraints before start");
     if (s->n <= 0 || !mass_ptr) return s->fail(TITAN_GB300_EINVAL, "set masses first");
@@ -1273,9 +1318,11 @@ int titan_gb300_set_local_constraints(titan_gb300_sim *s, const int64_t *mass_pt
         s->lc_ptr[i + 1] = (int64_t)s->lc_type.size();
     }
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double offset, double fk, double fs) {
+int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double offset, double fk, double fs) try {
     if (!s || !normal) return TITAN_GB300_EINVAL;
     if ((int)s->planes.size() >= tg::kMaxPlanes) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global planes");
     double nn = norm3(normal);
@@ -1283,25 +1330,31 @@ int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double off
     s->planes.push_back({normal[0] / nn, normal[1] / nn, normal[2] / nn, offset, fk, fs});
     if (s->started) return upload_params(s);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_add_ball(titan_gb300_sim *s, const double center[3], double radius) {
+int titan_gb300_add_ball(titan_gb300_sim *s, const double center[3], double radius) try {
     if (!s || !center) return TITAN_GB300_EINVAL;
     if ((int)s->balls.size() >= tg::kMaxBalls) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global balls");
     s->balls.push_back({center[0], center[1], center[2], radius});
     if (s->started) return upload_params(s);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_clear_constraints(titan_gb300_sim *s) {
+int titan_gb300_clear_constraints(titan_gb300_sim *s) try {
     if (!s) return TITAN_GB300_EINVAL;
     s->planes.clear();
     s->balls.clear();
     if (s->started) return upload_params(s);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) {
+int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (kind < tg::INTEG_EULER || kind > tg::INTEG_RK2)
         return s->fail(TITAN_GB300_EINVAL, "integrator must be 0 (Euler), 1 (Verlet) or 2 (RK2)");
@@ -1327,9 +1380,11 @@ int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) {
     else if (!s->use_pipe && !s->use_async)
         CK(tg::step_prepare(s->prec, s->step_variant, kind, s->smem), "set shared memory");
     return upload_params(s);
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) {
+int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!(dt > 0)) return s->fail(TITAN_GB300_EINVAL, "Cannot set time step to negative or zero value.");
     s->dt = dt;
@@ -1338,18 +1393,22 @@ int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) {
         return upload_params(s);
     }
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 double titan_gb300_get_time_step(const titan_gb300_sim *s) { return s ? s->dt : 0.0; }
 
-int titan_gb300_set_global_acc(titan_gb300_sim *s, const double g[3]) {
+int titan_gb300_set_global_acc(titan_gb300_sim *s, const double g[3]) try {
     if (!s || !g) return TITAN_GB300_EINVAL;
     for (int c = 0; c < 3; c++) s->g[c] = g[c];
     if (s->started) return upload_params(s);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_set_bodies(titan_gb300_sim *s, int64_t nbodies, const int64_t *mass_ptr) {
+int titan_gb300_set_bodies(titan_gb300_sim *s, int64_t nbodies, const int64_t *mass_ptr) try {
     if (!s) return TITAN_GB300_EINVAL;
     s->plan_adopted = false;  // the topology may change
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set bodies before start");
@@ -1361,10 +1420,12 @@ int titan_gb300_set_bodies(titan_gb300_sim *s, int64_t nbodies, const int64_t *m
     s->body_plane.assign(nbodies, {0, 0, 1, 0, 0, 0});
     s->body_has_plane.assign(nbodies, 0);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_set_body_plane(titan_gb300_sim *s, int64_t body, const double normal[3], double offset,
-                               double fk, double fs) {
+                               double fk, double fs) try {
     if (!s || !normal) return TITAN_GB300_EINVAL;
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "set body planes before start");
     if (body < 0 || body >= (int64_t)s->body_plane.size()) return s->fail(TITAN_GB300_EINVAL, "no such body");
@@ -1373,9 +1434,11 @@ int titan_gb300_set_body_plane(titan_gb300_sim *s, int64_t body, const double no
     s->body_plane[body] = {normal[0] / nn, normal[1] / nn, normal[2] / nn, offset, fk, fs};
     s->body_has_plane[body] = 1;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_start(titan_gb300_sim *s, int tile_masses) {
+int titan_gb300_start(titan_gb300_sim *s, int tile_masses) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (s->n <= 0)
         return s->fail(TITAN_GB300_EINVAL, "No masses have been added. Please add masses before starting the simulation.");
@@ -1392,9 +1455,11 @@ int titan_gb300_start(titan_gb300_sim *s, int tile_masses) {
     if (rc) return rc;
     s->started = true;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
+int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (nsteps < 0) return s->fail(TITAN_GB300_EINVAL, "negative step count");
@@ -1463,16 +1528,20 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) {
     }
     s->steps += nsteps;
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_synchronize(titan_gb300_sim *s) {
+int titan_gb300_synchronize(titan_gb300_sim *s) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->stream) return TITAN_GB300_OK;
     CK(cudaStreamSynchronize(s->stream), "synchronize");
     return check_kernel_error(s);
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_poll(titan_gb300_sim *s) {
+int titan_gb300_poll(titan_gb300_sim *s) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->stream) return TITAN_GB300_OK;
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
@@ -1480,9 +1549,11 @@ int titan_gb300_poll(titan_gb300_sim *s) {
     if (e == cudaErrorNotReady) return TITAN_GB300_EBUSY;
     if (e != cudaSuccess) return s->cuda_fail(e, "poll");
     return check_kernel_error(s);
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_wait(titan_gb300_sim *s, double timeout_ms) {
+int titan_gb300_wait(titan_gb300_sim *s, double timeout_ms) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!(timeout_ms >= 0)) return s->fail(TITAN_GB300_EINVAL, "timeout must be >= 0");
     const auto t0 = std::chrono::steady_clock::now();
@@ -1493,9 +1564,11 @@ int titan_gb300_wait(titan_gb300_sim *s, double timeout_ms) {
         if (ms >= timeout_ms) return s->fail(TITAN_GB300_ETIMEOUT, "queued steps still running at the time limit");
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_device) {
+int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_device) try {
     if (!s || !out) return TITAN_GB300_EINVAL;
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
@@ -1518,9 +1591,11 @@ int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_devic
        "export vertices");
     CK(cudaStreamSynchronize(s->stream), "export vertices");
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_device) {
+int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_device) try {
     if (!s || !out) return TITAN_GB300_EINVAL;
     std::vector<uint32_t> idx(2 * (size_t)s->ns, 0);
     for (int64_t j = 0; j < s->ns; j++) {
@@ -1538,6 +1613,8 @@ int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_dev
     if (!idx.empty())
         CK(cudaMemcpy(out, idx.data(), idx.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "export indices");
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 double titan_gb300_time(const titan_gb300_sim *s) { return s ? s->T : 0.0; }
@@ -1557,17 +1634,19 @@ void titan_gb300_host_free(void *p) {
     if (p) cudaFreeHost(p);
 }
 
-int titan_gb300_set_time(titan_gb300_sim *s, double T) {
+int titan_gb300_set_time(titan_gb300_sim *s, double T) try {
     if (!s) return TITAN_GB300_EINVAL;
     s->T = T;
     if (!s->started) return TITAN_GB300_OK;
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
     return upload_params(s);
+} catch (...) {
+    return host_exception(s);
 }
 int64_t titan_gb300_steps(const titan_gb300_sim *s) { return s ? s->steps : 0; }
 
 int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx, double *pos, double *vel,
-                           double *acc, double *T) {
+                           double *acc, double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (count < 0 || count > s->n) return s->fail(TITAN_GB300_EINVAL, "bad count");
@@ -1611,16 +1690,20 @@ int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx
         if (outs[q] && !direct[q]) par_memcpy(outs[q], s->h_xfer + 3 * q * count, 3 * count * 8);
     if (T) mass_times(s, idx, count, T);
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_get_state(titan_gb300_sim *s, double *pos, double *vel, double *acc, double *T) {
+int titan_gb300_get_state(titan_gb300_sim *s, double *pos, double *vel, double *acc, double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
     return titan_gb300_get_masses(s, s->n, nullptr, pos, vel, acc, T);
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t *idx, const double *pos,
                                const double *vel, const double *m, const double *ext, const uint8_t *fixed,
-                               const double *drag, const double *T) {
+                               const double *drag, const double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!idx) count = s->n;
@@ -1713,11 +1796,13 @@ int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t 
         CK(cudaStreamSynchronize(s->stream), "set");
     }
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64_t *idx, const double *k,
                                   const double *rest, const double *damping, const int32_t *type,
-                                  const double *omega, const double *amp, const double *phase) {
+                                  const double *omega, const double *amp, const double *phase) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!idx) count = s->ns;
     if (count < 0 || count > s->ns) return s->fail(TITAN_GB300_EINVAL, "bad count");
@@ -1774,9 +1859,11 @@ int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64
             }
     }
     return upload_entries(s);
+} catch (...) {
+    return host_exception(s);
 }
 
-int titan_gb300_diagnostics(titan_gb300_sim *s, double g_mag, double energy[4], double momentum[6]) {
+int titan_gb300_diagnostics(titan_gb300_sim *s, double g_mag, double energy[4], double momentum[6]) try {
     if (!s) return TITAN_GB300_EINVAL;
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
@@ -1828,6 +1915,8 @@ int titan_gb300_diagnostics(titan_gb300_sim *s, double g_mag, double energy[4], 
     if (momentum)
         for (int c = 0; c < 6; c++) momentum[c] = out[3 + c];
     return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
 }
 
 void *titan_gb300_stream(titan_gb300_sim *s) { return s ? (void *)s->stream : nullptr; }
