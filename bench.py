@@ -113,9 +113,22 @@ def profiled_traffic(precision: str):
         return None
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+KERNEL_NAMES = {"warp-specialised": "k_step_ws", "per-tile": "k_step",
+                "per-tile-async": "k_step_async", "pull": "k_step_pull"}
 
+
+class ClockSampler:
+    """SM clocks and throttle reasons sampled while the timed region runs.
+
+    NVML is read through ctypes (libnvidia-ml.so.1) every millisecond from a
+    host thread, so that even a region of a few milliseconds is sampled (the
+    engine's calls release the interpreter lock while they wait); without
+    NVML, nvidia-smi polls every 10 ms.  Read-only queries: no GPU setting
+    is changed."""
+
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
@@ -123,18 +136,67 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.thread = None
+        self.samples = []  # (sm_mhz, max_mhz, reasons set)
+        self.source = None
+
+    def _nvml_handle(self):
+        import ctypes
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return None, None
+        h = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.device)
+            dom, b, d = getattr(pr, "pci_domain_id", None), getattr(pr, "pci_bus_id", None), getattr(pr, "pci_device_id", None)
+            if b is not None:
+                bus = f"{dom or 0:08x}:{b:02x}:{d or 0:02x}.0".encode()
+        except Exception:
+            bus = None
+        if bus is None or nv.nvmlDeviceGetHandleByPciBusId_v2(bus, ctypes.byref(h)) != 0:
+            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.device), ctypes.byref(h)) != 0:
+                return None, None
+        return nv, h
+
+    def _poll_nvml(self, nv, h):
+        import ctypes
+        clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))  # NVML_CLOCK_SM
+        while not self._stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and get_reasons(h, ctypes.byref(rs)) == 0:
+                self.samples.append((float(clk.value), float(mx.value),
+                                     {v for b, v in self.REASONS.items() if rs.value & b}))
+            self._stop.wait(0.001)
 
     def __enter__(self):
+        import threading
+        self._stop = threading.Event()
         try:
+            nv, h = self._nvml_handle()
+        except Exception:
+            nv, h = None, None
+        if nv is not None:
+            self.source = "nvml, 1 ms"
+            self.thread = threading.Thread(target=self._poll_nvml, args=(nv, h), daemon=True)
+            self.thread.start()
+            return self
+        try:
+            self.source = "nvidia-smi, 10 ms"
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "10"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
+        if self.thread is not None:
+            self._stop.set()
+            self.thread.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -142,27 +204,45 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
                 out = ""
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for ln in out.splitlines():
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) < 7:
+                    continue
+                try:
+                    sm, mx = float(parts[0]), float(parts[1])
+                except ValueError:
+                    continue
+                self.samples.append((sm, mx, {nm for nm, v in zip(names, parts[3:7]) if v.lower().startswith("active")}))
 
     def summary(self):
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        sm, mx, reasons = [], [], set()
-        for ln in getattr(self, "lines", []):
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 7:
-                continue
-            try:
-                sm.append(float(parts[0]))
-                mx.append(float(parts[1]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[3:7]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": self.source}
+        reasons = set()
+        for _, _, r in self.samples:
+            reasons |= r
+        return {"sm_mhz": statistics.median(x[0] for x in self.samples),
+                "sm_max_mhz": max(x[1] for x in self.samples), "reasons": sorted(reasons),
+                "samples": len(self.samples), "source": self.source}
+
+
+def workload_config(side, nm, ns, world):
+    """The `config` of the JSON line: the workload only, identical in both
+    arms (engine details go under "engine")."""
+    return {"workload": f"single {side}^3 lattice, {nm} masses, {ns} springs, 20% actuated, plane + ball, dt=1e-4",
+            "masses": nm, "springs": ns, "step": "one time step of the whole lattice",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "per-step working set larger than L2 (no flush)"}
+
+
+def mapped_repo_libraries():
+    """Shared libraries of this repository mapped into this process."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    libs = {ln.split()[-1] for ln in maps if ln.rstrip().endswith(".so") and str(ROOT) in ln}
+    return sorted(str(Path(x).relative_to(ROOT)) for x in libs)
 
 
 def cpu_oracle_rate(sc, steps, threads):
@@ -242,6 +322,8 @@ def run_ours(a, rank, world, local):
     info = sim.plan_info()
     kinfo = sim.kernel_info()
     sim.step(a.warmup)
+    # the graphs step(a.steps) replays are built before the timed region
+    sim.prepare_steps(a.steps)
     sim.synchronize()
     with ClockSampler(local) as clk:
         ms = timed(sim, a.steps)
@@ -254,25 +336,32 @@ def run_ours(a, rank, world, local):
     value = replica_value(ns * a.steps, world, ms_max / 1e3)
     traffic = profiled_traffic(a.precision)
 
-    # end to end through the C ABI with host buffers (page-locked, so the ABI
-    # moves them by DMA without its staging copy)
-    pos_h = tg.pinned_empty(sc["pos"].shape)
-    pos_h[:] = sc["pos"]
-    vel_h = tg.pinned_empty(sc["pos"].shape)
-    vel_h[:] = 0.0
-    out = {"pos": tg.pinned_empty(sc["pos"].shape)}
-    sim.set_mass_state(None, pos=pos_h, vel=vel_h)
-    sim.step(a.e2e_chunk)
-    sim.get_state(pos=True, vel=False, out=out)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(a.e2e_calls):
+    def e2e(sim, chunk, calls):
+        """Same metric end to end through the C ABI with host buffers: upload
+        of positions and velocities from page-locked host arrays (moved by
+        DMA, no staging copy), step(chunk), download of positions."""
+        pos_h = tg.pinned_empty(sc["pos"].shape)
+        pos_h[:] = sc["pos"]
+        vel_h = tg.pinned_empty(sc["pos"].shape)
+        vel_h[:] = 0.0
+        out = {"pos": tg.pinned_empty(sc["pos"].shape)}
         sim.set_mass_state(None, pos=pos_h, vel=vel_h)
-        sim.step(a.e2e_chunk)
+        sim.step(chunk)
         sim.get_state(pos=True, vel=False, out=out)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    barrier()
-    e2e_val = ns * a.e2e_chunk * a.e2e_calls * world / e2e_s
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            sim.set_mass_state(None, pos=pos_h, vel=vel_h)
+            sim.step(chunk)
+            sim.get_state(pos=True, vel=False, out=out)
+        secs = max_over_ranks(time.perf_counter() - t0, world)
+        barrier()
+        return {"value": ns * chunk * calls * world / secs, "unit": UNIT, "h2d_bytes_per_step": 6 * nm * 8 / chunk,
+                "d2h_bytes_per_step": 3 * nm * 8 / chunk, "steps_per_call": chunk, "calls": calls,
+                "path": "C ABI: set_mass_state(page-locked host pos+vel) -> step(chunk) -> "
+                        "get_state(page-locked host pos)"}
+
+    e2e_main = e2e(sim, a.e2e_chunk, a.e2e_calls)
     sim.close()
 
     fp64 = None
@@ -280,11 +369,14 @@ def run_ours(a, rank, world, local):
         s64 = wl.make_sim(sc, tg.FP64, 0, device=local)
         i64 = s64.plan_info()
         s64.step(3)
+        s64.prepare_steps(a.fp64_steps)
         s64.synchronize()
         ms64 = timed(s64, a.fp64_steps)
         t = ms64 / a.fp64_steps / 1e3
         fp64 = {"value": ns / t, "unit": UNIT, "ms_per_step": ms64 / a.fp64_steps, "steps": a.fp64_steps,
                 "mass_updates_per_s": nm / t, "algorithmic_gbs": i64["algorithmic_bytes_per_step"] / t / 1e9,
+                "kernel": s64.kernel_info()["kernel"],
+                "e2e": e2e(s64, a.e2e_chunk, max(1, a.e2e_calls // 2)),
                 "note": "FP64 drop-in (bit-identical to the CPU oracle); FP64-ALU bound on GB300"}
         s64.close()
 
@@ -306,28 +398,23 @@ def run_ours(a, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": a.precision, "data": "synthetic (seeded actuated lattice on a frictional plane)",
-        "config": {"workload": f"single {a.side}^3 lattice, {nm} masses, {ns} springs, 20% actuated, "
-                               "plane + ball, dt=1e-4", "masses": nm, "springs": ns,
-                   "precision": a.precision, "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "per-step working set larger than L2 (no flush)", "tiles": info["tiles"],
-                   "kernel": kinfo["kernel"], "ctas": kinfo["ctas"], "threads_per_cta": kinfo["threads"],
-                   "smem_bytes": kinfo["smem_bytes"]},
+        "config": workload_config(a.side, nm, ns, world),
+        "engine": {"precision": a.precision, "tiles": info["tiles"], "kernel": kinfo["kernel"], "ctas": kinfo["ctas"],
+                   "threads_per_cta": kinfo["threads"], "smem_bytes": kinfo["smem_bytes"],
+                   "graphs": "built before the timed region (prepare_steps)"},
         "mass_updates_per_s": nm * a.steps * world / (ms_max / 1e3),
         "hbm_algorithmic_gbs": achieved,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
                      "implementation_bytes_per_launch": info["implementation_bytes_per_step"],
-                     "kernel": {"warp-specialised": "k_step_ws", "per-tile": "k_step", "pipelined": "k_step_pipe",
-                                "per-tile-async": "k_step_async"}.get(kinfo["kernel"], kinfo["kernel"])
+                     "kernel": KERNEL_NAMES.get(kinfo["kernel"], kinfo["kernel"])
                      + " (fused spring forces + mass update, one launch per step)"},
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * nm * 8 / a.e2e_chunk,
-                "d2h_bytes_per_step": 3 * nm * 8 / a.e2e_chunk, "steps_per_call": a.e2e_chunk,
-                "calls": a.e2e_calls,
-                "path": "C ABI: set_mass_state(page-locked host pos+vel) -> step(chunk) -> get_state(page-locked host pos)"},
+        "e2e": e2e_main,
         "gpu_launches": a.steps,
         "clocks": clk.summary(),
         "finite": finite,
+        "native_libraries": mapped_repo_libraries(),
     }
     if fp64:
         res["fp64"] = fp64
@@ -339,12 +426,17 @@ def run_ours(a, rank, world, local):
 
 
 def run_reference(a, rank, world):
+    """The reference arm: the reference's per-spring / per-mass functions
+    restated on the host (the oracle port, OpenMP, FP64 atomics as the
+    reference's kernels use), on all host threads, on the same workload.  The
+    scene is built with the oracle's own lattice builder, so no library of
+    the engine is loaded into this process."""
     if rank != 0:
         return None
-    from titan_gb300 import workloads as wl
     from oracle import pyoracle as po
-    sc = wl.actuated_lattice(a.side)
-    ns = sc["left"].size
+    from titan_gb300 import workloads as wl
+    sc = wl.actuated_lattice(a.side, lattice_fn=po.lattice)
+    ns, nm = sc["left"].size, sc["pos"].shape[0]
     threads = os.cpu_count() or 1
     o = po.OracleSim(sc)
     o.step(min(a.warmup, 3), po.ATOMIC_OMP, threads)
@@ -356,13 +448,13 @@ def run_reference(a, rank, world):
     return {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded actuated lattice on a frictional plane)",
-            "config": {"workload": f"single {a.side}^3 lattice, {sc['pos'].shape[0]} masses, {ns} springs, "
-                                   "20% actuated, plane + ball, dt=1e-4", "precision": "f64"},
+            "config": workload_config(a.side, nm, ns, world),
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{k} of the {a.steps} requested full steps (each the whole lattice), "
                                        "reference per-spring/per-mass functions restated in C, OpenMP atomics"},
-            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "native_libraries": mapped_repo_libraries()}
 
 
 def _event_ms(sim, steps, local):

@@ -63,7 +63,11 @@ public:
     Cube *createCube(const Vec &center, double side_length);
     Lattice *createLattice(const Vec &center, const Vec &dims, int nx = 10, int ny = 10, int nz = 10);
     Beam *createBeam(const Vec &center, const Vec &dims, int nx = 10, int ny = 10, int nz = 10);
-    // STL voxelisation is not part of this engine; throws std::runtime_error.
+    // Binary STL import (src/sim.cu:1855-1921): a num_pts^3 lattice over the
+    // mesh's bounding box, keeping the masses whose point the mesh contains
+    // (ray-parity point-in-mesh test on the GPU, seeded rays) and the springs
+    // between them.  Throws std::runtime_error when the file cannot be read
+    // or is not a binary STL.
     Container *importFromSTL(const std::string &path, double density = 10.0, int num_rays = 5);
 
     // Bulk modifications, host objects only

@@ -233,6 +233,13 @@ int titan_gb300_resident_info(const titan_gb300_sim *sim, int64_t out[8]);
  * replayed from cached CUDA graphs.  Asynchronous. */
 int titan_gb300_step(titan_gb300_sim *sim, int64_t nsteps);
 
+/* Extension (no counterpart in the reference, whose execute() loop launches
+ * kernels directly): builds and caches the CUDA graphs that step(nsteps)
+ * would replay from the current step parity, without launching anything, so
+ * that a later step(nsteps) spends no host time on graph capture.  Graphs
+ * are dropped when the scene is rebuilt (integrator switch, topology change). */
+int titan_gb300_prepare_steps(titan_gb300_sim *sim, int64_t nsteps);
+
 /* Wait for queued work; replaces the cudaDeviceSynchronize at src/sim.cu:1570. */
 int titan_gb300_synchronize(titan_gb300_sim *sim);
 

@@ -22,7 +22,7 @@ REF=${TITAN_REFERENCE:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 NVCC=${NVCC:-nvcc}
-[ -f "$REF/src/object.cu" ] || { echo "reference sources not found at $REF" >&2; exit 1; }
+[ -f "$REF/src/object.cu" ] || { echo "reference sources not found at $REF (set TITAN_REFERENCE)" >&2; exit 3; }
 mkdir -p "$OUT/obj"
 FLAGS=(-std=c++17 -O2 -DCONSTRAINTS -rdc=true -maxrregcount=64 -Xcompiler -fPIC,-ffp-contract=off
        -gencode arch=compute_103a,code=sm_103a

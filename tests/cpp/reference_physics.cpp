@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <iostream>
 #include <map>
 #include <string>
@@ -250,14 +251,58 @@ static void topology_edit_test() {
     sim.stop();
 }
 
+// deleteSpring / deleteMass / deleteContainer while paused (src/sim.cu:
+// 351-410, 510-563): a 6^3 lattice and a 4^3 lattice fall onto a
+// frictional plane; after the first pause four springs of the first lattice,
+// one of its masses (whose springs are then skipped, src/sim.cu:1052) and the
+// whole second lattice are deleted, and the run resumes.  The remaining
+// masses' state is written to the file named on the command line
+// (int64 steps before and after the deletion, int64 mass count, then pos
+// and vel of each mass in sim.masses order, doubles) for the oracle to check.
+static const char *g_dump_path = nullptr;
+static void delete_after_start_test() {
+    titan::Simulation sim;
+    titan::Lattice *a = sim.createLattice(Vec(0, 0, 0.6), Vec(1, 1, 1), 6, 6, 6);
+    titan::Lattice *b = sim.createLattice(Vec(3, 0, 0.6), Vec(1, 1, 1), 4, 4, 4);
+    sim.createPlane(Vec(0, 0, 1), 0, 0.5, 0.5);
+    sim.start();
+    sim.pause(0.05);
+    const int64_t n1 = sim.steps();
+    for (int j : {0, 7, 100, 333}) sim.deleteSpring(a->springs[j]);
+    sim.deleteMass(a->masses[40]);
+    sim.deleteContainer(b);
+    EXPECT_TRUE(sim.masses.size() == 215);
+    sim.resume();
+    sim.pause(0.2);
+    const int64_t n2 = sim.steps() - n1;
+    sim.getAll();
+    EXPECT_TRUE(g_dump_path != nullptr);
+    if (!g_dump_path) return;
+    FILE *f = std::fopen(g_dump_path, "wb");
+    EXPECT_TRUE(f != nullptr);
+    if (!f) return;
+    const int64_t head[3] = {n1, n2, (int64_t)sim.masses.size()};
+    std::fwrite(head, 8, 3, f);
+    for (titan::Mass *m : sim.masses) {
+        const double rec[6] = {m->pos[0], m->pos[1], m->pos[2], m->vel[0], m->vel[1], m->vel[2]};
+        std::fwrite(rec, 8, 6, f);
+    }
+    std::fclose(f);
+    sim.stop();
+}
+
 // importFromSTL (src/sim.cu:1855-1921): a binary STL of an L-shaped solid
 // (two closed boxes, [0,2]x[0,1]x[0,1] and [0,1]x[1,2]x[0,1]) written here;
 // the bounding box [0,2]x[0,2]x[0,1] gets a 10^3 lattice, and the masses in
 // the missing quadrant are dropped with their springs.
 static void stl_import_test() {
-    const char *path = "/tmp/titan_gb300_stl_import_test.stl";
+    // a per-run file name, so that concurrent runs do not share the fixture
+    char path[] = "/tmp/titan_gb300_stl_XXXXXX";
     {
-        FILE *f = std::fopen(path, "wb");
+        const int fd = mkstemp(path);
+        EXPECT_TRUE(fd >= 0);
+        if (fd < 0) return;
+        FILE *f = fdopen(fd, "wb");
         EXPECT_TRUE(f != nullptr);
         if (!f) return;
         char header[80] = {0};
@@ -376,11 +421,13 @@ int main(int argc, char **argv) {
         {"beam_fixed_face_test", beam_fixed_face_test},
         {"topology_edit_test", topology_edit_test},
         {"stl_import_test", stl_import_test},
+        {"delete_after_start_test", delete_after_start_test},
     };
     if (argc < 2 || !tests.count(argv[1])) {
         for (auto &kv : tests) std::printf("%s\n", kv.first.c_str());
         return argc < 2 ? 0 : 2;
     }
+    if (argc > 2) g_dump_path = argv[2];
     try {
         tests[argv[1]]();
     } catch (const std::exception &e) {

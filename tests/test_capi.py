@@ -53,9 +53,9 @@ DT = {"new2old": np.int32, "tile_mass_off": np.int64, "tile_halo_off": np.int64,
       "body_of_tile": np.int32, "tile_nh": np.int32}
 
 
-def plan_tables(sc, tile, precision=tg.FP32C):
+def plan_tables(sc, tile, precision=tg.FP32C, kernel=0):
     s = tg.Sim(precision)
-    wl.load(s, sc, start=False)
+    wl.load(s, sc, start=False, kernel=kernel)
     rc = s._L.titan_gb300_plan_host(s._h, tile)
     s._check(rc, "plan_host")
     out = {}
@@ -196,8 +196,9 @@ def test_plan_tiles_are_compact_blocks():
 
 def test_plan_default_tile_adapts_and_keeps_small_bodies_whole():
     """Default tiles: a small lattice gets tiles small enough to cover the
-    SMs; bodies that fit the large-scene tile (208 masses in FP32C) are one
-    tile each even then."""
+    SMs; bodies that fit the large-scene tile (208 masses in FP32C, where
+    the warp-specialised kernel runs) are one tile each even then; a large
+    lattice gets the 208-mass tiles."""
     small = wl.lattice_scene((0, 0, 1), (1, 1, 1), 20, 20, 20)
     P = plan_tables(small, 0)
     nm = np.diff(P["tile_mass_off"])
@@ -211,6 +212,9 @@ def test_plan_default_tile_adapts_and_keeps_small_bodies_whole():
         ntile = int(np.sum(body_of_tile == b))
         if sizes[b] <= 208:
             assert ntile == 1, (b, sizes[b], ntile)
+    plain = wl.lattice_scene((0, 0, 1), (1, 1, 1), 64, 64, 64)
+    d, p208 = plan_tables(plain, 0), plan_tables(plain, 208)
+    assert all(np.array_equal(d[k], p208[k]) for k in d)
 
 
 def denser_lattice(n, extra=1, seed=1):
@@ -245,10 +249,10 @@ def test_plan_default_tile_falls_back_when_two_stages_do_not_fit():
     192 when two stages of the 208-mass tiles would not fit one SM's shared
     memory (checked on the host from the plan itself)."""
     plain = wl.lattice_scene((0, 0, 1), (1, 1, 1), 52, 52, 52)
-    d, p208 = plan_tables(plain, 0), plan_tables(plain, 208)
+    d, p208 = plan_tables(plain, 0, kernel=4), plan_tables(plain, 208, kernel=4)
     assert all(np.array_equal(d[k], p208[k]) for k in d)
     dense = denser_lattice(52)
-    d, p192, p208 = plan_tables(dense, 0), plan_tables(dense, 192), plan_tables(dense, 208)
+    d, p192, p208 = plan_tables(dense, 0, kernel=4), plan_tables(dense, 192, kernel=4), plan_tables(dense, 208, kernel=4)
     assert all(np.array_equal(d[k], p192[k]) for k in d)
     assert p208["tile_mass_off"].size < p192["tile_mass_off"].size
 

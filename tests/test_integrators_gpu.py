@@ -66,11 +66,11 @@ def test_fp32c_free_flight_error_and_forms(integ):
     ref.step(5000)
     want = ref.get_state()["pos"]
     got = {}
-    for kernel in (1, 3, 4):
+    for kernel in (1, 3, 4, 6):
         s = wl.make_sim(sc, tg.FP32C, 0, kernel=kernel)
         s.step(5000)
         got[kernel] = s.get_state(acc=True)
     assert np.max(np.abs(got[1]["pos"] - want)) < 1e-6
-    for kernel in (3, 4):
+    for kernel in (3, 4, 6):
         for k in ("pos", "vel", "acc"):
             assert np.array_equal(got[1][k], got[kernel][k]), (kernel, k)

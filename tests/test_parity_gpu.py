@@ -147,37 +147,53 @@ def kernel_scenes():
     wl.actuate(lat, rng, 0.3, 0.1)
     lat["planes"].append(((0.0, 0.1, 1.0), 0.0, 0.4, 0.6))
     lat["balls"].append(((0.3, 0.0, -0.1), 0.35))
-    return {"lattice": lat, "hub": hub_scene(degree=300), "bodies": wl.robot_batch(nbodies=24, seed=9, side_range=(3, 7))}
+    # damping that differs between springs (the pull form's per-column path)
+    var = wl.lattice_scene((0, 0, 0.55), (1.0, 0.8, 0.9), 9, 7, 8, k=2e3, damping=0.2)
+    var["vel"] = rng.normal(scale=0.5, size=var["pos"].shape)
+    var["damping"] = rng.uniform(0.0, 0.4, var["damping"].size)
+    var["damping"][::5] = 0.0
+    wl.actuate(var, rng, 0.3, 0.1)
+    var["planes"].append(((0.0, 0.0, 1.0), 0.0, 0.5, 0.5))
+    return {"lattice": lat, "hub": hub_scene(degree=300), "bodies": wl.robot_batch(nbodies=24, seed=9, side_range=(3, 7)),
+            "damping": var}
 
 
 @pytest.mark.parametrize("precision", [tg.FP64, tg.FP32, tg.FP32C])
-@pytest.mark.parametrize("scene", ["lattice", "hub", "bodies"])
+@pytest.mark.parametrize("scene", ["lattice", "hub", "bodies", "damping"])
 @pytest.mark.parametrize("tile", [32, 96])
 def test_kernel_forms_bitwise_identical(precision, scene, tile):
-    """The pipelined persistent kernel (TMA-staged tiles), the per-tile
-    kernel and the per-tile kernel with asynchronous staging give identical
-    bits in every precision."""
+    """The per-tile kernel, the per-tile kernel with asynchronous staging,
+    the warp-specialised kernel and (FP32 and FP32C) the pull kernel give
+    identical bits; the pull kernel refuses a scene with a heavy mass."""
     sc = kernel_scenes()[scene]
     s1, a = gpu_run(sc, 700, precision, tile=tile, kernel=1, resident=(0, 0, 0))
-    s2, b = gpu_run(sc, 700, precision, tile=tile, kernel=2, resident=(0, 0, 0))
     s3, c = gpu_run(sc, 700, precision, tile=tile, kernel=3, resident=(0, 0, 0))
     s4, d = gpu_run(sc, 700, precision, tile=tile, kernel=4, resident=(0, 0, 0))
-    assert s1.kernel_info()["kernel"] == "per-tile" and s2.kernel_info()["kernel"] == "pipelined"
-    assert s3.kernel_info()["kernel"] == "per-tile-async" and s4.kernel_info()["kernel"] == "warp-specialised"
+    assert s1.kernel_info()["kernel"] == "per-tile" and s3.kernel_info()["kernel"] == "per-tile-async"
+    assert s4.kernel_info()["kernel"] == "warp-specialised"
+    others = [c, d]
+    if precision != tg.FP64:
+        if scene == "hub":
+            with pytest.raises(tg.TitanError, match="ELIMIT"):
+                gpu_run(sc, 1, precision, tile=tile, kernel=6, resident=(0, 0, 0))
+        else:
+            s6, e = gpu_run(sc, 700, precision, tile=tile, kernel=6, resident=(0, 0, 0))
+            assert s6.kernel_info()["kernel"] == "pull"
+            others.append(e)
     for k in ("pos", "vel", "acc", "T"):
-        assert np.array_equal(a[k], b[k]), k
-        assert np.array_equal(a[k], c[k]), k
-        assert np.array_equal(a[k], d[k]), k
+        for o in others:
+            assert np.array_equal(a[k], o[k]), k
 
 
-def test_pipelined_kernel_with_few_ctas_per_tile_list():
-    """Tiles walked by a persistent grid (pipelined and warp-specialised
-    forms): more tiles than CTAs, odd counts."""
+@pytest.mark.parametrize("precision", [tg.FP64, tg.FP32C])
+def test_persistent_kernels_with_more_tiles_than_ctas(precision):
+    """Tiles walked by a persistent grid (warp-specialised and pull forms):
+    more tiles than CTAs, odd counts, partial units."""
     sc = wl.lattice_scene((0, 0, 1.0), (2, 2, 2), 41, 39, 37, k=3e3, damping=0.1)
     sc["planes"].append(((0.0, 0.0, 1.0), 0.0, 0.5, 0.5))
-    _, a = gpu_run(sc, 300, tg.FP64, tile=32, kernel=1)
-    for form in (2, 4):
-        s, b = gpu_run(sc, 300, tg.FP64, tile=32, kernel=form)
+    _, a = gpu_run(sc, 300, precision, tile=48, kernel=1)
+    for form in ((4, 6) if precision != tg.FP64 else (4,)):
+        s, b = gpu_run(sc, 300, precision, tile=48, kernel=form)
         info = s.kernel_info()
         assert info["ctas"] < s.plan_info()["tiles"]
         assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])

@@ -71,6 +71,7 @@ _SIGS = {
     "titan_gb300_set_resident": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "titan_gb300_resident_info": (ctypes.c_int, [_P, _I64]),
     "titan_gb300_step": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "titan_gb300_prepare_steps": (ctypes.c_int, [_P, ctypes.c_int64]),
     "titan_gb300_synchronize": (ctypes.c_int, [_P]),
     "titan_gb300_poll": (ctypes.c_int, [_P]),
     "titan_gb300_wait": (ctypes.c_int, [_P, ctypes.c_double]),
@@ -310,15 +311,17 @@ class Sim:
         self._check(self._L.titan_gb300_set_occupancy(self._h, min_ctas_per_sm), "set_occupancy")
 
     def set_kernel(self, variant: int):
-        """0 automatic, 1 per-tile kernel, 2 pipelined persistent kernel, 3 per-tile
-        kernel with asynchronous (bulk-copy) staging, 4 warp-specialised
-        persistent kernel (producer warp + consumer warps, stage ring)."""
+        """0 automatic, 1 per-tile kernel, 3 per-tile kernel with asynchronous
+        (bulk-copy) staging, 4 warp-specialised persistent kernel (producer
+        warp + consumer warps, stage ring of slabs), 6 pull kernel (FP32 and
+        FP32C: every mass sums its own springs' forces from streamed spring
+        columns against tile states staged by a producer warp)."""
         self._check(self._L.titan_gb300_set_kernel(self._h, variant), "set_kernel")
 
     def kernel_info(self) -> dict:
         out = np.zeros(4, np.int64)
         self._check(self._L.titan_gb300_kernel_info(self._h, _ptr(out, ctypes.c_int64)), "kernel_info")
-        names = {1: "per-tile", 2: "pipelined", 3: "per-tile-async", 4: "warp-specialised", 5: "resident-tiles"}
+        names = {1: "per-tile", 3: "per-tile-async", 4: "warp-specialised", 5: "resident-tiles", 6: "pull"}
         return {"kernel": names.get(int(out[0]), "per-tile"), "ctas": int(out[1]), "threads": int(out[2]),
                 "smem_bytes": int(out[3])}
 
@@ -350,6 +353,10 @@ class Sim:
 
     def step(self, nsteps: int = 1):
         self._check(self._L.titan_gb300_step(self._h, nsteps), "step")
+
+    def prepare_steps(self, nsteps: int):
+        """Build the CUDA graphs a later step(nsteps) replays, launching nothing."""
+        self._check(self._L.titan_gb300_prepare_steps(self._h, nsteps), "prepare_steps")
 
     def poll(self) -> bool:
         """True when every queued step has finished."""

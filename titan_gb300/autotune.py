@@ -16,11 +16,12 @@ from pathlib import Path
 from . import FP64, Sim
 from . import workloads as wl
 
-# (kernel form, tile masses, threads per CTA); form 4 = warp-specialised
-# (threads = consumer threads), 3 = per-tile with asynchronous staging,
-# 1 = per-tile
-CANDIDATES_F32 = [(4, 208, 448), (4, 192, 448), (4, 176, 448), (4, 160, 448), (4, 112, 448), (3, 256, 256),
-                  (1, 256, 256), (1, 128, 128)]
+# (kernel form, tile masses, threads per CTA); form 6 = pull (threads =
+# consumer threads: a team of one warp per 32 tile masses per tile in
+# flight; 0 = two teams), 4 = warp-specialised (threads = consumer
+# threads), 3 = per-tile with asynchronous staging, 1 = per-tile
+CANDIDATES_F32 = [(6, 256, 0), (6, 192, 0), (6, 128, 0), (6, 128, 384), (4, 208, 448), (4, 192, 448),
+                  (4, 160, 448), (3, 256, 256), (1, 256, 256), (1, 128, 128)]
 CANDIDATES_F64 = [(1, 128, 128), (1, 64, 128), (3, 128, 128), (1, 128, 256)]
 
 

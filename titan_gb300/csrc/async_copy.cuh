@@ -43,6 +43,29 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(__cvta_generic_to_global(src))
                  : "memory");
 }
+// Arrives on bar once this thread's earlier cp.async copies have landed
+// (the barrier's expected count includes this arrival).
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait on an mbarrier phase; gives up early when another warp
+// raised the abort word.  sleep_ns > 0 backs off between polls (a producer
+// that runs ahead waits this way so that its polling does not take issue
+// slots from the consumers on its scheduler).
+__device__ __forceinline__ bool bounded_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word,
+                                             unsigned sleep_ns = 0) {
+    for (uint32_t it = 0; it < kWaitLimit; it++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *abort_word) return false;
+        if (sleep_ns) __nanosleep(sleep_ns);
+    }
+    return false;
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }

@@ -125,10 +125,13 @@ struct titan_gb300_sim {
     int threads_req = 0;  // CTA size override (0: derived from the tile size)
     int min_ctas_req = 0; // register cap of the per-tile kernel: 0/1 none, 3 or 4 CTAs per SM
     int step_variant = 0; // launch-bound variant in use (engine.h)
-    int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 2 pipelined kernel, 3 per-tile with async staging
-    bool use_pipe = false;
+    int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 3 per-tile with async staging, 4 warp-specialised, 6 pull
     bool use_async = false;
     bool use_ws = false;
+    bool use_pull = false;
+    tg::PullTables pull;  // host copy of the pull form's spring tables
+    std::vector<tg::PullTile> pull_tiles;
+    int64_t pull_impl_bytes = 0;
     int ws_warps = 0;     // consumer warps of the warp-specialised kernel
     int ctas = 0;         // persistent grid of the pipelined kernel
     int *d_err = nullptr;
@@ -155,7 +158,7 @@ struct titan_gb300_sim {
     cudaError_t launch(int parity, int write_acc, int stage = 0) {
         if (args.ntiles == 0) return cudaSuccess;
         args.rk2_stage = stage;
-        if (use_pipe) return tg::launch_step_pipe(prec, args, ctas, threads, parity, write_acc, stream);
+        if (use_pull) return tg::launch_step_pull(prec, integrator, args, ctas, parity, write_acc, stream);
         if (use_ws) return tg::launch_step_ws(prec, integrator, args, ctas, ws_warps, parity, write_acc, stream);
         if (use_async)
             return tg::launch_step_async(prec, args, (int)args.ntiles, threads, smem, parity, write_acc, stream);
@@ -352,6 +355,18 @@ int upload_mass_attrs(titan_gb300_sim *s) {
     return TITAN_GB300_OK;
 }
 
+tg::PullSprings pull_springs(const titan_gb300_sim *s) {
+    tg::PullSprings sp;
+    sp.k = s->k.data();
+    sp.rest = s->rest.data();
+    sp.damping = s->damping.empty() ? nullptr : s->damping.data();
+    sp.type = s->type.empty() ? nullptr : s->type.data();
+    sp.omega = s->omega.empty() ? nullptr : s->omega.data();
+    sp.amp = s->amp.empty() ? nullptr : s->amp.data();
+    sp.phase = s->phase.empty() ? nullptr : s->phase.data();
+    return sp;
+}
+
 // Spring records (slab-entry layout: FP64 k, rest, damping, word; FP32
 // word, k, rest, damping) and actuation records for the springs spring[e]
 // with entry words word[e] (spring -1: a zero padding record), uploaded to
@@ -410,6 +425,24 @@ int upload_entries(titan_gb300_sim *s) {
     auto &a = s->args;
     int rc = upload_records(s, P.ent_spring, P.ent_ends, const_cast<void *>(a.ent), const_cast<void *>(a.act));
     if (rc) return rc;
+    if (s->use_pull && a.pull_units) {  // new spring parameters: same layout, new values
+        tg::PullTables T;
+        std::string why = tg::build_pull(P, s->pull_tiles, pull_springs(s), T);
+        if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
+        if (T.units.size() != s->pull.units.size() || T.ell.size() != s->pull.ell.size() ||
+            T.act.size() != s->pull.act.size())
+            return s->fail(TITAN_GB300_EINVAL, "pull tables changed shape without a new plan");
+        s->pull = std::move(T);
+        CK(cudaMemcpy(const_cast<tg::PullUnit *>(a.pull_units), s->pull.units.data(),
+                      s->pull.units.size() * sizeof(tg::PullUnit), cudaMemcpyHostToDevice),
+           "upload pull units");
+        CK(cudaMemcpy(const_cast<uint8_t *>(a.pull_ell), s->pull.ell.data(), s->pull.ell.size(),
+                      cudaMemcpyHostToDevice),
+           "upload pull columns");
+        CK(cudaMemcpy(const_cast<float4 *>(a.pull_act), s->pull.act.data(), s->pull.act.size() * sizeof(float),
+                      cudaMemcpyHostToDevice),
+           "upload pull actuation");
+    }
     if (s->use_res)
         rc = upload_records(s, s->rplan.rec_spring, s->rplan.words, const_cast<void *>(s->rargs.rec),
                             const_cast<void *>(s->rargs.act));
@@ -428,6 +461,27 @@ T *dev_copy(titan_gb300_sim *s, const std::vector<T> &v, cudaError_t &e) {
 // stages of the default's tiles do not fit one SM's shared memory
 constexpr int kWsDefaultTile = 208;
 constexpr int kWsFallbackTile = 192;
+// default tile of the pull form: eight 32-mass units, one per warp of a team
+constexpr int kPullDefaultTile = 256;
+// the automatic kernel choice in FP32 and FP32C: the warp-specialised form
+// (measured faster on GB300: 0.121 against 0.26 ms per 100^3 step)
+constexpr bool kPullAuto = false;
+constexpr int kHeavyThreshold = 96;
+
+// Whether the step will run the pull form: when requested (set_kernel 6).
+// (It needs a plan without heavy masses: it has no warp-cooperative sums.)
+bool pull_wanted(const titan_gb300_sim *s) {
+    if (s->kernel_req == 6) return true;
+    if (!kPullAuto || s->kernel_req != 0 || s->prec == P_FP64) return false;
+    std::vector<int32_t> deg(s->n, 0);
+    for (int64_t j = 0; j < s->ns; j++) {
+        const int64_t l = s->left[j], r = s->right[j];
+        if (l < 0 || r < 0 || l >= s->n || r >= s->n) continue;
+        if (++deg[l] > kHeavyThreshold && (s->fixed.empty() || !s->fixed[l])) return false;
+        if (++deg[r] > kHeavyThreshold && (s->fixed.empty() || !s->fixed[r])) return false;
+    }
+    return true;
+}
 
 tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     tg::PlanInput in;
@@ -454,7 +508,8 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
     // against 28.9 resident).  Measured on GB300, 20^3 lattice: FP64 37 us
     // per step with 32-mass tiles against 90 with 256; FP32C 5.3 us with
     // 64 against 6.5 with 208.
-    const bool ws = s->kernel_req == 0 || s->kernel_req == 4;
+    const bool pull = pull_wanted(s);
+    const bool ws = !pull && (s->kernel_req == 0 || s->kernel_req == 4);
     if (tile_masses > 0) {
         in.tile_cap = tile_masses;
     } else {
@@ -469,6 +524,9 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
         };
         if (s->prec == P_FP64) {
             in.tile_cap = fit(1.6, 32, 256);  // small bodies split too: FP64 binds per SM
+        } else if (pull) {
+            in.tile_cap = fit(4.0, 64, kPullDefaultTile);
+            in.whole_cap = kPullDefaultTile;
         } else if (ws) {
             in.tile_cap = fit(4.0, 64, kWsDefaultTile);
             in.whole_cap = kWsDefaultTile;
@@ -476,7 +534,7 @@ tg::PlanInput plan_input(titan_gb300_sim *s, int tile_masses) {
             in.tile_cap = 256;
         }
     }
-    in.heavy_threshold = 96;
+    in.heavy_threshold = kHeavyThreshold;
     // a tile's staged state, entry forces and heavy sums share one CTA's
     // shared memory (tile_smem_bytes)
     const int rs = (int)s->rsize();
@@ -571,13 +629,103 @@ void ws_stage_layout(int prec, const std::vector<tg::TileInfo> &tiles, tg::WsLay
     W.nstages = (int32_t)std::min<int64_t>(tg::kWsMaxStages, room / std::max<int64_t>(1, W.stage));
 }
 
+// Shared-memory layout of the pull kernel for these tiles (sized by their
+// largest): stages of one tile's state records, as many as fit one SM (at
+// most kPullMaxStages, a multiple of the team count, at least two per
+// team).  Returns false when that many do not fit.
+bool pull_layout(int prec, const std::vector<tg::TileInfo> &tiles, int threads_req, tg::PullLayout &L) {
+    auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
+    const int rec = tg::state_record_bytes(prec);
+    int64_t mS = 0, mNm = 0, mNh = 0;
+    for (const tg::TileInfo &ti : tiles) {
+        mS = std::max<int64_t>(mS, ti.nm + ti.nh);
+        mNm = std::max<int64_t>(mNm, ti.nm);
+        mNh = std::max<int64_t>(mNh, ti.nh);
+    }
+    L = tg::PullLayout{};
+    L.team_warps = (int32_t)std::max<int64_t>(1, (mNm + 31) / 32);
+    if (L.team_warps > tg::kPullMaxConsumerWarps) return false;
+    // two teams by default (one team's narrow tile start and end overlap
+    // the other's streaming); set_launch's thread count asks for another
+    const int want = threads_req > 0 ? threads_req / 32 / L.team_warps : 2;
+    L.nteams = std::max(1, std::min(want, tg::kPullMaxConsumerWarps / L.team_warps));
+    L.stage = (int32_t)al(mS * rec, 128);
+    L.idx_words = (int32_t)al(std::max<int64_t>(mNh, 1), 4);
+    const int64_t tail = 2 * (int64_t)L.idx_words * 4 + al((int64_t)sizeof(tg::DevParams), 16) +
+                         (2 * tg::kPullMaxStages + 2) * 8 + 32 + 32;
+    const int64_t room = 227 * 1024 - tail;
+    int64_t ns = std::min<int64_t>(tg::kPullMaxStages, room / std::max<int64_t>(1, L.stage));
+    ns -= ns % L.nteams;
+    if (ns < 2 * L.nteams) return false;
+    L.nstages = (int32_t)ns;
+    L.idx = (int32_t)(ns * L.stage);
+    L.params = (int32_t)al(L.idx + 2 * (int64_t)L.idx_words * 4, 16);
+    L.mbar = (int32_t)al(L.params + (int64_t)sizeof(tg::DevParams), 16);
+    L.total = L.mbar + (2 * L.nstages + 2) * 8 + 32;
+    return L.total <= 227 * 1024;
+}
+
+// Builds the pull form's tables and layout for the tiles the per-step
+// kernel runs; on success sets use_pull and each tile's first unit (pad0).
+// A scene the pull form cannot run is an error only when it was requested.
+int setup_pull(titan_gb300_sim *s, std::vector<tg::TileInfo> &tiles_run) {
+    s->use_pull = false;
+    if (s->prec == P_FP64) return s->fail(TITAN_GB300_EINVAL, "the pull kernel runs FP32 and FP32C only");
+    std::vector<tg::PullTile> pt(tiles_run.size());
+    for (size_t t = 0; t < tiles_run.size(); t++) {
+        pt[t].mass_off = tiles_run[t].mass_off;
+        pt[t].ent_off = tiles_run[t].ent_off;
+        pt[t].warp_off = tiles_run[t].warp_off;
+        pt[t].nm = tiles_run[t].nm;
+    }
+    tg::PullLayout L{};
+    if (!pull_layout(s->prec, tiles_run, s->threads_req, L)) {
+        if (s->kernel_req == 6) return s->fail(TITAN_GB300_ELIMIT, "two tiles per team do not fit the pull kernel's shared memory");
+        return TITAN_GB300_OK;
+    }
+    std::string why = tg::build_pull(s->plan, pt, pull_springs(s), s->pull);
+    if (!why.empty()) {
+        s->pull = tg::PullTables();
+        if (s->kernel_req == 6) return s->fail(TITAN_GB300_ELIMIT, why);
+        return TITAN_GB300_OK;
+    }
+    for (size_t t = 0; t < tiles_run.size(); t++) tiles_run[t].pad0 = s->pull.tile_unit_off[t];
+    s->pull_tiles = std::move(pt);
+    s->args.pull = L;
+    // implementation bytes of one step: state records read (tile and halo)
+    // and written, m, flags and degree per mass, the spring columns of every
+    // lane's degree, actuation records and headers, unit descriptors, halo
+    // indices and tile records
+    const int64_t rec = tg::state_record_bytes(s->prec);
+    int64_t cols = 0, dcols = 0, nh = 0;
+    for (size_t t = 0; t < tiles_run.size(); t++) {
+        nh += tiles_run[t].nh;
+        for (int i = 0; i < tiles_run[t].nm; i++) {
+            const int d = s->plan.deg[tiles_run[t].mass_off + i];
+            cols += d;
+            if (s->pull.units[s->pull.tile_unit_off[t] + i / 32].flags & tg::PU_DAMP) dcols += d;
+        }
+    }
+    int64_t acts = 0;
+    for (const tg::PullUnit &pu : s->pull.units) {
+        const uint16_t *off = reinterpret_cast<const uint16_t *>(s->pull.act.data() + 4 * (size_t)pu.act);
+        acts += off[32];
+    }
+    int64_t nm = 0;
+    for (const tg::PullTile &p : s->pull_tiles) nm += p.nm;
+    s->pull_impl_bytes = nm * (2 * rec + 4 + 2) + nh * (rec + 4) + cols * 10 + dcols * 4 + acts * 16 +
+                         (int64_t)s->pull.units.size() * (16 + 32) + (int64_t)tiles_run.size() * (int64_t)sizeof(tg::TileInfo);
+    s->use_pull = true;
+    return TITAN_GB300_OK;
+}
+
 // Builds s->plan for a requested tile size (0: the default).  The default
 // tile of the warp-specialised form (208 masses) gives way to 192 when two
 // stages of the planned tiles would not fit one SM's shared memory.
 std::string plan_scene(titan_gb300_sim *s, int tile_masses, tg::PlanInput &in) {
     in = plan_input(s, tile_masses);
     std::string why = tg::build_plan(in, s->plan);
-    if (why.empty() && tile_masses == 0 && in.tile_cap == kWsDefaultTile) {
+    if (why.empty() && tile_masses == 0 && in.tile_cap == kWsDefaultTile && !pull_wanted(s)) {
         tg::WsLayout W{};
         ws_stage_layout(s->prec, tile_infos(s->plan), W);
         if (W.nstages < 2) {
@@ -619,7 +767,6 @@ int build_device(titan_gb300_sim *s) {
     a.hcap = std::max(P.max_heavy, 1);
     cudaError_t e = cudaSuccess;
     s->smem = 0;
-    int64_t max_ne = 0, max_nact = 0, max_incw = 0, max_nh = 0, max_slots = 0, max_heavy = 0;
     std::vector<tg::TileInfo> tiles = tile_infos(P);
     for (int64_t t = 0; t < P.ntiles; t++) {
         const tg::TileInfo &ti = tiles[t];
@@ -627,12 +774,6 @@ int build_device(titan_gb300_sim *s) {
         s->smem = std::max(s->smem, s->kernel_req == 3
                                         ? tg::tile_async_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy)
                                         : tg::tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy));
-        max_ne = std::max<int64_t>(max_ne, ti.ne);
-        max_nact = std::max<int64_t>(max_nact, ti.nact);
-        max_incw = std::max<int64_t>(max_incw, ti.inc_words);
-        max_nh = std::max<int64_t>(max_nh, ti.nh);
-        max_slots = std::max<int64_t>(max_slots, ti.nm + ti.nh);
-        max_heavy = std::max<int64_t>(max_heavy, ti.nheavy);
     }
     if (P.inc.size() > (size_t)INT32_MAX) return s->fail(TITAN_GB300_ELIMIT, "incidence table exceeds 2^31 words");
     // body-resident bins: whole bodies that fit one CTA run all the steps of
@@ -724,29 +865,22 @@ int build_device(titan_gb300_sim *s) {
     std::vector<tg::TileInfo> tiles_run;
     for (int64_t t = 0; t < P.ntiles; t++)
         if ((!s->use_res || !s->rplan.tile_resident[t]) && !rt_flag[t]) tiles_run.push_back(tiles[t]);
-    // shared-memory layout of the pipelined kernel (two stages)
-    {
-        auto al = [](int64_t x) { return (int32_t)((x + 15) & ~int64_t(15)); };
-        const int rec = tg::state_record_bytes(s->prec), ent = tg::entry_record_bytes(s->prec);
-        tg::PipeLayout &L = a.pipe;
-        L.rec = 0;
-        L.act = al(max_ne * ent);
-        L.inc = L.act + al(max_nact * ent);
-        L.st = L.inc + al(max_incw * 2);
-        L.stage = L.st + al(max_slots * rec);
-        L.idx = 2 * L.stage;
-        L.idx_bytes = al(((max_nh + 3) & ~int64_t(3)) * 4);
-        L.heavy = L.idx + 2 * L.idx_bytes;
-        L.mbar = al(L.heavy + 3 * max_heavy * (int64_t)rs);
-        L.tinfo = L.mbar + 16;
-        L.total = L.tinfo + tg::kPipeTileCache * (int32_t)sizeof(tg::TileInfo);
-    }
     // automatic choice: the warp-specialised form in FP32 and FP32C (measured
     // fastest on GB300, see the kernel-form sweep in profiles/) when two of
     // the scene's tiles fit one SM's shared memory, else the per-tile form;
     // the per-tile form in FP64 (FP64-ALU bound, no gain from overlap)
+    // the pull form when requested (or automatic, kPullAuto), else the
+    // warp-specialised one
+    s->use_pull = false;
+    s->pull = tg::PullTables();
+    s->pull_tiles.clear();
+    if ((s->kernel_req == 6 || (kPullAuto && s->kernel_req == 0 && s->prec != P_FP64)) && !tiles_run.empty()) {
+        int rc = setup_pull(s, tiles_run);
+        if (rc) return rc;
+    }
     s->use_ws = false;
-    const bool want_ws = s->kernel_req == 4 || (s->kernel_req == 0 && s->prec != P_FP64 && !tiles_run.empty());
+    const bool want_ws =
+        !s->use_pull && (s->kernel_req == 4 || (s->kernel_req == 0 && s->prec != P_FP64 && !tiles_run.empty()));
     if (want_ws) {
         tg::WsLayout &W = a.ws;
         ws_stage_layout(s->prec, tiles_run, W);
@@ -772,19 +906,13 @@ int build_device(titan_gb300_sim *s) {
         s->threads = (s->ws_warps + 1) * 32;
         s->use_ws = true;
     }
-    s->use_pipe = s->kernel_req == 2 && a.pipe.total <= 227 * 1024;
-    if (s->kernel_req == 2 && !s->use_pipe)
-        return s->fail(TITAN_GB300_ELIMIT, "tiles too large for the pipelined kernel's two shared-memory stages");
-    if (s->use_pipe) {
-        // a persistent CTA computes every slab entry of its tiles: give it
-        // more warps than a tile has masses
-        if (s->threads_req == 0) s->threads = std::max(256, s->threads);
-        CK(tg::step_pipe_prepare(s->prec, (size_t)a.pipe.total), "set shared memory");
-        int sms = 0, dev = 0, per_sm = 1;
+    if (s->use_pull) {
+        CK(tg::step_pull_prepare(s->prec, s->integrator, (size_t)a.pull.total), "set shared memory");
+        int sms = 0, dev = 0;
         CK(cudaGetDevice(&dev), "device");
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
-        per_sm = std::max(1, (227 * 1024) / a.pipe.total);
-        s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), (int64_t)sms * per_sm);
+        s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), sms);
+        s->threads = (a.pull.nteams * a.pull.team_warps + 1) * 32;
     } else if (!s->use_ws) {
         if (s->smem > 227 * 1024) return s->fail(TITAN_GB300_ELIMIT, "tile does not fit in shared memory");
         s->use_async = s->kernel_req == 3;
@@ -809,6 +937,13 @@ int build_device(titan_gb300_sim *s) {
         dst = p_;                                             \
     } while (0)
     DEVCOPY(a.tiles, tiles_run, "upload tiles");
+    if (s->use_pull) {
+        DEVCOPY(a.pull_units, s->pull.units, "upload pull units");
+        DEVCOPY(a.pull_ell, s->pull.ell, "upload pull columns");
+        const float *act = nullptr;
+        DEVCOPY(act, s->pull.act, "upload pull actuation");
+        a.pull_act = reinterpret_cast<const float4 *>(act);
+    }
     if (s->use_rtiles) DEVCOPY(s->rtargs.tiles, s->rtiles, "upload resident tiles");
     if (s->use_res) {
         tg::ResPlan &R = s->rplan;
@@ -1073,7 +1208,8 @@ int titan_gb300_set_occupancy(titan_gb300_sim *s, int min_ctas_per_sm) try {
 
 int titan_gb300_set_kernel(titan_gb300_sim *s, int variant) try {
     if (!s) return TITAN_GB300_EINVAL;
-    if (variant < 0 || variant > 4) return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0 to 4");
+    if (variant < 0 || variant > 6 || variant == 2 || variant == 5)
+        return s->fail(TITAN_GB300_EINVAL, "kernel variant must be 0, 1, 3, 4 or 6");
     if (s->started) return s->fail(TITAN_GB300_ESTATE, "choose the kernel before start");
     s->kernel_req = variant;
     return TITAN_GB300_OK;
@@ -1090,10 +1226,10 @@ int titan_gb300_kernel_info(const titan_gb300_sim *s, int64_t out[4]) {
         out[3] = (int64_t)s->rt_smem;
         return TITAN_GB300_OK;
     }
-    out[0] = s->use_pipe ? 2 : (s->use_async ? 3 : (s->use_ws ? 4 : 1));
-    out[1] = (s->use_pipe || s->use_ws) ? s->ctas : s->args.ntiles;
+    out[0] = s->use_pull ? 6 : (s->use_async ? 3 : (s->use_ws ? 4 : 1));
+    out[1] = (s->use_ws || s->use_pull) ? s->ctas : s->args.ntiles;
     out[2] = s->threads;
-    out[3] = s->use_pipe ? s->args.pipe.total : (s->use_ws ? s->args.ws.total : (int64_t)s->smem);
+    out[3] = s->use_pull ? s->args.pull.total : (s->use_ws ? s->args.ws.total : (int64_t)s->smem);
     return TITAN_GB300_OK;
 }
 
@@ -1375,9 +1511,11 @@ int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) try {
         return build_device(s);
     }
     // the kernels of the new integrator need their shared-memory limit
-    if (s->use_ws)
+    if (s->use_pull)
+        CK(tg::step_pull_prepare(s->prec, kind, (size_t)s->args.pull.total), "set shared memory");
+    else if (s->use_ws)
         CK(tg::step_ws_prepare(s->prec, kind, (size_t)s->args.ws.total), "set shared memory");
-    else if (!s->use_pipe && !s->use_async)
+    else if (!s->use_async)
         CK(tg::step_prepare(s->prec, s->step_variant, kind, s->smem), "set shared memory");
     return upload_params(s);
 } catch (...) {
@@ -1527,6 +1665,27 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) try {
         for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
     }
     s->steps += nsteps;
+    return TITAN_GB300_OK;
+} catch (...) {
+    return host_exception(s);
+}
+
+int titan_gb300_prepare_steps(titan_gb300_sim *s, int64_t nsteps) try {
+    if (!s) return TITAN_GB300_EINVAL;
+    if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
+    if (nsteps < 0) return s->fail(TITAN_GB300_EINVAL, "negative step count");
+    if (s->args.ntiles == 0 || nsteps <= 1) return TITAN_GB300_OK;
+    if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
+    // the same chunk sequence step(nsteps) replays, from the current parity
+    cudaError_t e = cudaSuccess;
+    const int P = s->passes();
+    int parity = s->parity;
+    for (int64_t rem = nsteps - 1; rem > 0;) {
+        const int len = (int)std::min<int64_t>(rem, kChunk);
+        if (!get_graph(s, len, parity, e)) return s->cuda_fail(e, "build step graph");
+        parity ^= ((len * P) & 1);
+        rem -= len;
+    }
     return TITAN_GB300_OK;
 } catch (...) {
     return host_exception(s);
@@ -1956,7 +2115,7 @@ int titan_gb300_plan_info(const titan_gb300_sim *s, int64_t out[12]) {
     impl += (int64_t)P.ent_ends.size() * (f64 ? 32 : 16) + nact_ent * (f64 ? 32 : 16);
     impl += (int64_t)P.inc.size() * 2 + (int64_t)P.heavy_inc.size() * 2 + (int64_t)P.halo.size() * 4;
     impl += P.ntiles * (int64_t)sizeof(tg::TileInfo);
-    out[10] = impl;
+    out[10] = s->use_pull ? s->pull_impl_bytes : impl;
     out[11] = nact_ent;
     return TITAN_GB300_OK;
 }

@@ -21,6 +21,8 @@
 
 #include <cuda_runtime.h>
 
+#include "pull_layout.h"
+
 namespace tg {
 
 enum { P_FP64 = 0, P_FP32 = 1, P_FP32C = 2 };
@@ -36,17 +38,6 @@ struct TileInfo {
     int32_t inc_words, pad0, pad1, pad2;       // inc_words: length of that block (multiple of 128)
 };
 
-// Shared-memory layout of the pipelined step kernel (byte offsets).  Two
-// stages, each holding one tile's slab records, actuation records,
-// incidence block and state records (tile masses, then halo masses); two
-// halo-index buffers; heavy-mass sums; two mbarriers.
-struct PipeLayout {
-    int32_t rec, act, inc, st, stage;  // offsets inside a stage, stage size
-    int32_t idx, idx_bytes;            // first halo-index buffer, size of one
-    int32_t heavy, mbar, tinfo, total; // tinfo: cached TileInfo of the CTA's first kPipeTileCache tiles
-};
-constexpr int kPipeTileCache = 64;
-
 // Shared-memory layout of the warp-specialised persistent kernel
 // (step_ws.cu): nstages stages, each [state records | slab records / force
 // slots | actuation records | incidence block], the two-entry halo-index
@@ -60,6 +51,20 @@ struct WsLayout {
 };
 constexpr int kWsMaxStages = 3;
 constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
+
+// Shared-memory layout of the pull kernel (step_pull.cu): nstages stages of
+// one tile's state records (tile masses, then halo), the two-entry
+// halo-index ring, a copy of the DevParams, 2 * nstages + 2 mbarriers and
+// the control words.  Consumer warps form nteams teams of team_warps warps
+// (one warp per 32 tile masses); team q takes the CTA's tiles q, q + nteams,
+// ... in stages k % nstages (nstages a multiple of nteams).
+struct PullLayout {
+    int32_t stage, nstages, nteams, team_warps;
+    int32_t idx, idx_words;        // halo-index ring (2 entries of idx_words int32)
+    int32_t params, mbar, total;
+};
+constexpr int kPullMaxStages = 12;
+constexpr int kPullMaxConsumerWarps = 16;  // + the producer warp: 544 threads
 
 enum { INTEG_EULER = 0, INTEG_VERLET = 1, INTEG_RK2 = 2 };
 
@@ -113,8 +118,13 @@ struct StepArgs {
     int32_t ntiles;
     int32_t rk2_stage;         // RK2: 0 first half step, 1 second (launches alternate)
     int *err;                  // set by a kernel whose bounded wait gave up
-    PipeLayout pipe;
     WsLayout ws;
+    // pull form: per-unit descriptors (a tile's units start at its
+    // TileInfo::pad0), unit blocks and actuation records (pull_layout.h)
+    const PullUnit *pull_units;
+    const uint8_t *pull_ell;
+    const float4 *pull_act;
+    PullLayout pull;
 };
 
 // Body-resident batched launch (resident.cu, plan.h ResPlan): bins of whole
@@ -193,11 +203,6 @@ const void *step_kernel_capped(int precision, int variant);  // null if not comp
 cudaError_t step_prepare(int precision, int variant, int integ, size_t smem);
 cudaError_t launch_step(int precision, int variant, int integ, const StepArgs &a, int ntiles, int threads,
                         size_t smem, int parity, int write_acc, cudaStream_t s);
-// Pipelined persistent variant (step_tma.cu): grid of `ctas` CTAs walking the
-// tiles, TMA bulk copies of the next tile overlapping the current tile.
-cudaError_t step_pipe_prepare(int precision, size_t smem);
-cudaError_t launch_step_pipe(int precision, const StepArgs &a, int ctas, int threads, int parity, int write_acc,
-                             cudaStream_t s);
 // Per-tile kernel with asynchronous staging (step_async.cu): slab records and
 // tile states by bulk copy, halo by cp.async, one wait.  Shared memory per
 // CTA: tile_async_smem_bytes.
@@ -211,6 +216,11 @@ cudaError_t launch_step_async(int precision, const StepArgs &a, int ntiles, int 
 cudaError_t step_ws_prepare(int precision, int integ, size_t smem);
 cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas, int consumer_warps, int parity,
                            int write_acc, cudaStream_t s);
+// Pull kernel (step_pull.cu): `ctas` persistent CTAs of a.pull's teams
+// plus a producer warp; FP32 and FP32C only.
+cudaError_t step_pull_prepare(int precision, int integ, size_t smem);
+cudaError_t launch_step_pull(int precision, int integ, const StepArgs &a, int ctas, int parity, int write_acc,
+                             cudaStream_t s);
 // bytes of one state record / one slab entry record for a precision
 int state_record_bytes(int precision);
 int entry_record_bytes(int precision);

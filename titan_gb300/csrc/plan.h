@@ -14,6 +14,8 @@
 #include <string>
 #include <vector>
 
+#include "pull_layout.h"
+
 namespace tg {
 
 struct PlanInput {
@@ -108,5 +110,30 @@ struct ResPlan {
 // 254 (free masses only count) and no spring to another body, and packs
 // them into bins of bin_cap masses (bin_cap >= max_masses).
 void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_cap, ResPlan &R);
+
+// Spring tables of the pull form (pull_layout.h), derived from a tile plan
+// for the tiles the per-step kernel runs.  A tile's units are 32 consecutive
+// tile masses each; lane l of unit u lists the springs of tile mass 32u + l
+// in its incidence order (ascending spring index), each as the other end's
+// tile-local slot and the spring's k, rest, damping and actuation, in the
+// FP32 forms' rounding.
+struct PullTile {
+    int64_t mass_off = 0, ent_off = 0, warp_off = 0;
+    int32_t nm = 0;
+};
+struct PullSprings {
+    const double *k = nullptr, *rest = nullptr, *damping = nullptr;
+    const int32_t *type = nullptr;  // null: all passive
+    const double *omega = nullptr, *amp = nullptr, *phase = nullptr;  // null: 0, 0.2, 0
+};
+struct PullTables {
+    std::vector<int32_t> tile_unit_off;  // per tile: its first unit
+    std::vector<PullUnit> units;
+    std::vector<uint8_t> ell;            // unit blocks
+    std::vector<float> act;              // 4 floats per 16-byte record (headers and records)
+};
+// Returns "" on success, else why the pull form cannot run the plan (a heavy
+// mass, whose incidence list the plan keeps apart); throws nothing.
+std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, const PullSprings &sp, PullTables &out);
 
 }  // namespace tg

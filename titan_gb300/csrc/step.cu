@@ -25,6 +25,8 @@ cudaError_t raise_smem_limit(const void *f, size_t smem) {
 }
 
 int state_words(int precision) { return precision == P_FP64 ? 6 : (precision == P_FP32C ? 12 : 8); }
+int state_record_bytes(int precision) { return precision == P_FP32 ? 32 : 48; }
+int entry_record_bytes(int precision) { return precision == P_FP64 ? 32 : 16; }
 
 size_t tile_smem_bytes(int precision, int slots, int entries, int heavy) {
     const int64_t rec = precision == P_FP32 ? 32 : 48;

@@ -46,14 +46,6 @@ constexpr int kWsThreads = (kWsMaxConsumerWarps + 1) * 32;
 template <int PREC>
 __host__ __device__ constexpr int ws_rec() { return PREC == P_FP32 ? 32 : 48; }
 
-// Arrives on bar once this thread's earlier cp.async copies have landed
-// (the barrier's expected count includes this arrival).
-__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 __device__ __forceinline__ void group_sync(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -66,20 +58,6 @@ __device__ __forceinline__ bool group_any(int id, int nthreads, bool v) {
         : "r"((uint32_t)v), "r"(id), "r"(nthreads)
         : "memory");
     return r != 0;
-}
-
-// Bounded wait; gives up early when another warp raised the abort word.
-// sleep_ns > 0 backs off between polls (the producer, which runs ahead,
-// waits this way so that its polling does not take issue slots from the
-// consumers on its scheduler).
-__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word,
-                                        unsigned sleep_ns = 0) {
-    for (uint32_t it = 0; it < kWaitLimit; it++) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u && *abort_word) return false;
-        if (sleep_ns) __nanosleep(sleep_ns);
-    }
-    return false;
 }
 
 template <int PREC, int INTEG>
@@ -155,9 +133,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
             const bool has_next = t + G < ntiles;
             TileInfo tn = {};
             if (has_next) tn = a.tiles[t + G];
-            bool ok = ws_wait(&empty[s], ph ^ 1u, abort_word, 200);
+            bool ok = bounded_wait(&empty[s], ph ^ 1u, abort_word, 200);
             if (ok) {
-                ok = ws_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
+                ok = bounded_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
                 if (ok && lane == 0) *idx_waited = k + 1;
             }
             if (__any_sync(0xffffffffu, !ok)) {
@@ -217,7 +195,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
         for (int k = grp, t = blockIdx.x + grp * G; t < ntiles; k += 2, t += 2 * G) {
             const int s = k % NS;
             const uint32_t ph = (uint32_t)(k / NS) & 1u;
-            const bool ok = ws_wait(&full[s], ph, abort_word);
+            const bool ok = bounded_wait(&full[s], ph, abort_word);
             if (group_any(bar_id, gn, !ok)) {
                 if (gt == 0) {
                     *abort_word = 1;

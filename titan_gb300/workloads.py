@@ -27,8 +27,12 @@ def empty_scene(dt=1e-4, g=(0.0, 0.0, -9.81)):
     return {"planes": [], "balls": [], "g": np.array(g, float), "dt": float(dt)}
 
 
-def lattice_scene(center, dims, nx, ny, nz, m=0.1, k=1e4, damping=0.0, dt=1e-4, g=(0.0, 0.0, -9.81)):
-    pos, left, right, rest = lattice(center, dims, nx, ny, nz)
+def lattice_scene(center, dims, nx, ny, nz, m=0.1, k=1e4, damping=0.0, dt=1e-4, g=(0.0, 0.0, -9.81),
+                  lattice_fn=None):
+    """lattice_fn(center, dims, nx, ny, nz) -> (pos, left, right, rest): the
+    geometry builder (default: the engine's titan_gb300.lattice; any builder
+    that reproduces createLattice gives the same scene)."""
+    pos, left, right, rest = (lattice_fn or lattice)(center, dims, nx, ny, nz)
     n, ns = pos.shape[0], left.size
     sc = empty_scene(dt, g)
     sc.update(pos=pos, vel=np.zeros_like(pos), m=np.full(n, m), left=left, right=right,
@@ -62,7 +66,7 @@ def actuate(sc, rng, fraction, amp, period=(0.1, 1.0), kinds=(2, 3)):
     return sc
 
 
-def actuated_lattice(n_side=100, seed=20261203):
+def actuated_lattice(n_side=100, seed=20261203, lattice_fn=None):
     """Single large lattice: n_side^3 masses (100^3 = 1,000,000 masses,
     12,731,796 springs), 5 m cube centred at (0,0,2.6) so its bottom face
     starts 0.1 m above the plane, m = 0.1 kg; k log-uniform in [1e3, 1e5],
@@ -73,7 +77,8 @@ def actuated_lattice(n_side=100, seed=20261203):
     0.1 kg mass at ~20 m/s per step, which would make precision comparisons
     measure chaos, not arithmetic); dt = 1e-4."""
     rng = np.random.default_rng(seed)
-    sc = lattice_scene((0.0, 0.0, 2.6), (5.0, 5.0, 5.0), n_side, n_side, n_side, m=0.1, damping=0.1)
+    sc = lattice_scene((0.0, 0.0, 2.6), (5.0, 5.0, 5.0), n_side, n_side, n_side, m=0.1, damping=0.1,
+                       lattice_fn=lattice_fn)
     ns = sc["left"].size
     sc["k"] = np.exp(rng.uniform(math.log(1e3), math.log(1e5), ns))
     actuate(sc, rng, 0.2, 0.1)
