@@ -360,10 +360,6 @@ tg::PullSprings pull_springs(const titan_gb300_sim *s) {
     sp.k = s->k.data();
     sp.rest = s->rest.data();
     sp.damping = s->damping.empty() ? nullptr : s->damping.data();
-    sp.type = s->type.empty() ? nullptr : s->type.data();
-    sp.omega = s->omega.empty() ? nullptr : s->omega.data();
-    sp.amp = s->amp.empty() ? nullptr : s->amp.data();
-    sp.phase = s->phase.empty() ? nullptr : s->phase.data();
     return sp;
 }
 
@@ -411,6 +407,7 @@ int upload_records(titan_gb300_sim *s, const std::vector<int64_t> &spring, const
             ac[4 * e] = (float)(sp_omega(j) / two_pi);
             ac[4 * e + 1] = (float)(ty == 2 ? -sp_amp(j) : sp_amp(j));
             ac[4 * e + 2] = (float)(sp_phase(j) / two_pi);
+            ac[4 * e + 3] = (float)s->rest[j];  // read by the pull form with the record
         }
         CK(cudaMemcpy(rec, ent.data(), ent.size() * 4, cudaMemcpyHostToDevice), "upload records");
         CK(cudaMemcpy(act, ac.data(), ac.size() * 4, cudaMemcpyHostToDevice), "upload actuation");
@@ -427,10 +424,10 @@ int upload_entries(titan_gb300_sim *s) {
     if (rc) return rc;
     if (s->use_pull && a.pull_units) {  // new spring parameters: same layout, new values
         tg::PullTables T;
-        std::string why = tg::build_pull(P, s->pull_tiles, pull_springs(s), T);
+        std::string why = tg::build_pull(P, s->pull_tiles, s->pull.team_warps, tg::state_record_bytes(s->prec) / 16,
+                                         pull_springs(s), T);
         if (!why.empty()) return s->fail(TITAN_GB300_ELIMIT, why);
-        if (T.units.size() != s->pull.units.size() || T.ell.size() != s->pull.ell.size() ||
-            T.act.size() != s->pull.act.size())
+        if (T.units.size() != s->pull.units.size() || T.ell.size() != s->pull.ell.size())
             return s->fail(TITAN_GB300_EINVAL, "pull tables changed shape without a new plan");
         s->pull = std::move(T);
         CK(cudaMemcpy(const_cast<tg::PullUnit *>(a.pull_units), s->pull.units.data(),
@@ -439,9 +436,6 @@ int upload_entries(titan_gb300_sim *s) {
         CK(cudaMemcpy(const_cast<uint8_t *>(a.pull_ell), s->pull.ell.data(), s->pull.ell.size(),
                       cudaMemcpyHostToDevice),
            "upload pull columns");
-        CK(cudaMemcpy(const_cast<float4 *>(a.pull_act), s->pull.act.data(), s->pull.act.size() * sizeof(float),
-                      cudaMemcpyHostToDevice),
-           "upload pull actuation");
     }
     if (s->use_res)
         rc = upload_records(s, s->rplan.rec_spring, s->rplan.words, const_cast<void *>(s->rargs.rec),
@@ -461,10 +455,12 @@ T *dev_copy(titan_gb300_sim *s, const std::vector<T> &v, cudaError_t &e) {
 // stages of the default's tiles do not fit one SM's shared memory
 constexpr int kWsDefaultTile = 208;
 constexpr int kWsFallbackTile = 192;
-// default tile of the pull form: eight 32-mass units, one per warp of a team
-constexpr int kPullDefaultTile = 256;
+// default tile of the pull form: seven 32-mass units, one per warp of a team
+// (two teams and the producer: 16 warps, four per SM sub-partition)
+constexpr int kPullDefaultTile = 224;
 // the automatic kernel choice in FP32 and FP32C: the warp-specialised form
-// (measured faster on GB300: 0.121 against 0.26 ms per 100^3 step)
+// (measured faster on GB300 on the 100^3 lattice: 0.121 ms per step against
+// 0.134 for the pull form with 160-mass tiles and three teams)
 constexpr bool kPullAuto = false;
 constexpr int kHeavyThreshold = 96;
 
@@ -636,11 +632,12 @@ void ws_stage_layout(int prec, const std::vector<tg::TileInfo> &tiles, tg::WsLay
 bool pull_layout(int prec, const std::vector<tg::TileInfo> &tiles, int threads_req, tg::PullLayout &L) {
     auto al = [](int64_t x, int64_t q) { return (x + q - 1) / q * q; };
     const int rec = tg::state_record_bytes(prec);
-    int64_t mS = 0, mNm = 0, mNh = 0;
+    int64_t mS = 0, mNm = 0, mNh = 0, mA = 0;
     for (const tg::TileInfo &ti : tiles) {
         mS = std::max<int64_t>(mS, ti.nm + ti.nh);
         mNm = std::max<int64_t>(mNm, ti.nm);
         mNh = std::max<int64_t>(mNh, ti.nh);
+        mA = std::max<int64_t>(mA, ti.nact);
     }
     L = tg::PullLayout{};
     L.team_warps = (int32_t)std::max<int64_t>(1, (mNm + 31) / 32);
@@ -649,7 +646,8 @@ bool pull_layout(int prec, const std::vector<tg::TileInfo> &tiles, int threads_r
     // the other's streaming); set_launch's thread count asks for another
     const int want = threads_req > 0 ? threads_req / 32 / L.team_warps : 2;
     L.nteams = std::max(1, std::min(want, tg::kPullMaxConsumerWarps / L.team_warps));
-    L.stage = (int32_t)al(mS * rec, 128);
+    L.act_off = (int32_t)al(mS * rec, 16);
+    L.stage = (int32_t)al(L.act_off + mA * 16, 128);
     L.idx_words = (int32_t)al(std::max<int64_t>(mNh, 1), 4);
     const int64_t tail = 2 * (int64_t)L.idx_words * 4 + al((int64_t)sizeof(tg::DevParams), 16) +
                          (2 * tg::kPullMaxStages + 2) * 8 + 32 + 32;
@@ -666,8 +664,8 @@ bool pull_layout(int prec, const std::vector<tg::TileInfo> &tiles, int threads_r
 }
 
 // Builds the pull form's tables and layout for the tiles the per-step
-// kernel runs; on success sets use_pull and each tile's first unit (pad0).
-// A scene the pull form cannot run is an error only when it was requested.
+// kernel runs; on success sets use_pull.  A scene the pull form cannot run
+// is an error only when it was requested.
 int setup_pull(titan_gb300_sim *s, std::vector<tg::TileInfo> &tiles_run) {
     s->use_pull = false;
     if (s->prec == P_FP64) return s->fail(TITAN_GB300_EINVAL, "the pull kernel runs FP32 and FP32C only");
@@ -683,38 +681,29 @@ int setup_pull(titan_gb300_sim *s, std::vector<tg::TileInfo> &tiles_run) {
         if (s->kernel_req == 6) return s->fail(TITAN_GB300_ELIMIT, "two tiles per team do not fit the pull kernel's shared memory");
         return TITAN_GB300_OK;
     }
-    std::string why = tg::build_pull(s->plan, pt, pull_springs(s), s->pull);
+    std::string why = tg::build_pull(s->plan, pt, L.team_warps, tg::state_record_bytes(s->prec) / 16,
+                                     pull_springs(s), s->pull);
     if (!why.empty()) {
         s->pull = tg::PullTables();
         if (s->kernel_req == 6) return s->fail(TITAN_GB300_ELIMIT, why);
         return TITAN_GB300_OK;
     }
-    for (size_t t = 0; t < tiles_run.size(); t++) tiles_run[t].pad0 = s->pull.tile_unit_off[t];
     s->pull_tiles = std::move(pt);
     s->args.pull = L;
     // implementation bytes of one step: state records read (tile and halo)
-    // and written, m, flags and degree per mass, the spring columns of every
-    // lane's degree, actuation records and headers, unit descriptors, halo
-    // indices and tile records
+    // and written, m and flags per mass, the spring quads of every unit
+    // (damping quads included where they are read), the tiles' actuation
+    // records, unit descriptors, halo indices and tile records
     const int64_t rec = tg::state_record_bytes(s->prec);
-    int64_t cols = 0, dcols = 0, nh = 0;
-    for (size_t t = 0; t < tiles_run.size(); t++) {
-        nh += tiles_run[t].nh;
-        for (int i = 0; i < tiles_run[t].nm; i++) {
-            const int d = s->plan.deg[tiles_run[t].mass_off + i];
-            cols += d;
-            if (s->pull.units[s->pull.tile_unit_off[t] + i / 32].flags & tg::PU_DAMP) dcols += d;
-        }
+    int64_t nh = 0, nm = 0, nact = 0, quad_bytes = 0;
+    for (const tg::TileInfo &ti : tiles_run) {
+        nh += ti.nh;
+        nm += ti.nm;
+        nact += ti.nact;
     }
-    int64_t acts = 0;
-    for (const tg::PullUnit &pu : s->pull.units) {
-        const uint16_t *off = reinterpret_cast<const uint16_t *>(s->pull.act.data() + 4 * (size_t)pu.act);
-        acts += off[32];
-    }
-    int64_t nm = 0;
-    for (const tg::PullTile &p : s->pull_tiles) nm += p.nm;
-    s->pull_impl_bytes = nm * (2 * rec + 4 + 2) + nh * (rec + 4) + cols * 10 + dcols * 4 + acts * 16 +
-                         (int64_t)s->pull.units.size() * (16 + 32) + (int64_t)tiles_run.size() * (int64_t)sizeof(tg::TileInfo);
+    for (const tg::PullUnit &pu : s->pull.units) quad_bytes += (int64_t)pu.nquads * tg::pull_quad_bytes(pu.flags & tg::PU_DAMP);
+    s->pull_impl_bytes = nm * (2 * rec + 4 + 1) + nh * (rec + 4) + quad_bytes + nact * 16 +
+                         (int64_t)s->pull.units.size() * 16 + (int64_t)tiles_run.size() * (int64_t)sizeof(tg::TileInfo);
     s->use_pull = true;
     return TITAN_GB300_OK;
 }
@@ -940,9 +929,6 @@ int build_device(titan_gb300_sim *s) {
     if (s->use_pull) {
         DEVCOPY(a.pull_units, s->pull.units, "upload pull units");
         DEVCOPY(a.pull_ell, s->pull.ell, "upload pull columns");
-        const float *act = nullptr;
-        DEVCOPY(act, s->pull.act, "upload pull actuation");
-        a.pull_act = reinterpret_cast<const float4 *>(act);
     }
     if (s->use_rtiles) DEVCOPY(s->rtargs.tiles, s->rtiles, "upload resident tiles");
     if (s->use_res) {

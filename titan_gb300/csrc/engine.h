@@ -53,18 +53,19 @@ constexpr int kWsMaxStages = 3;
 constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
 
 // Shared-memory layout of the pull kernel (step_pull.cu): nstages stages of
-// one tile's state records (tile masses, then halo), the two-entry
-// halo-index ring, a copy of the DevParams, 2 * nstages + 2 mbarriers and
-// the control words.  Consumer warps form nteams teams of team_warps warps
-// (one warp per 32 tile masses); team q takes the CTA's tiles q, q + nteams,
-// ... in stages k % nstages (nstages a multiple of nteams).
+// one tile's state records (tile masses, then halo) and its actuation
+// records (at act_off), the two-entry halo-index ring, a copy of the
+// DevParams, 2 * nstages + 2 mbarriers and the control words.  Consumer
+// warps form nteams teams of team_warps warps (one warp per 32 tile
+// masses); team q takes the CTA's tiles q, q + nteams, ... in stages
+// k % nstages (nstages a multiple of nteams).
 struct PullLayout {
-    int32_t stage, nstages, nteams, team_warps;
+    int32_t stage, act_off, nstages, nteams, team_warps;
     int32_t idx, idx_words;        // halo-index ring (2 entries of idx_words int32)
     int32_t params, mbar, total;
 };
 constexpr int kPullMaxStages = 12;
-constexpr int kPullMaxConsumerWarps = 16;  // + the producer warp: 544 threads
+constexpr int kPullMaxConsumerWarps = 15;  // + the producer warp: 512 threads (4 warps per SM sub-partition)
 
 enum { INTEG_EULER = 0, INTEG_VERLET = 1, INTEG_RK2 = 2 };
 
@@ -119,11 +120,10 @@ struct StepArgs {
     int32_t rk2_stage;         // RK2: 0 first half step, 1 second (launches alternate)
     int *err;                  // set by a kernel whose bounded wait gave up
     WsLayout ws;
-    // pull form: per-unit descriptors (a tile's units start at its
-    // TileInfo::pad0), unit blocks and actuation records (pull_layout.h)
+    // pull form: unit descriptors (pull.team_warps slots per tile) and
+    // their quad blocks (pull_layout.h)
     const PullUnit *pull_units;
     const uint8_t *pull_ell;
-    const float4 *pull_act;
     PullLayout pull;
 };
 

@@ -983,35 +983,27 @@ void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_
     for (int64_t t = 0; t < P.ntiles; t++) R.tile_resident[t] = R.resident[P.body_of_tile[t]];
 }
 
-std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, const PullSprings &sp,
-                       PullTables &T) try {
+std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, int team_warps, int rec_f4,
+                       const PullSprings &sp, PullTables &T) try {
     T = PullTables();
+    T.team_warps = team_warps;
     const int64_t nt = (int64_t)tiles.size();
-    T.tile_unit_off.resize(nt + 1);
-    int64_t nu = 0;
-    for (int64_t t = 0; t < nt; t++) {
-        T.tile_unit_off[t] = (int32_t)nu;
-        nu += (tiles[t].nm + 31) / 32;
-    }
-    T.tile_unit_off[nt] = (int32_t)nu;
-    if (nu > INT32_MAX) return "more than 2^31 units";
-    // pass 1: per unit its column count and actuated springs per lane
-    std::vector<int32_t> unit_tile(nu);
-    for (int64_t t = 0; t < nt; t++)
-        for (int64_t q = T.tile_unit_off[t]; q < T.tile_unit_off[t + 1]; q++) unit_tile[q] = (int32_t)t;
-    std::vector<uint16_t> ncols(nu, 0);
-    std::vector<uint32_t> nact(nu, 0);
-    std::vector<uint8_t> heavy(nu, 0);
-    const double kTwoPi = 6.283185307179586476925286766559;
+    const int64_t nu = nt * team_warps;
     auto code_of = [&](const PullTile &ti, int64_t u, int l, int j) {
         return P.inc[ell_index(P.warp_inc_off[ti.warp_off + u], (uint32_t)l, (uint32_t)j)];
     };
+    // pass 1: per unit slot its masses, columns and whether damping varies
+    std::vector<uint16_t> nq(nu, 0);
+    std::vector<uint8_t> lanes(nu, 0), damp(nu, 0), heavy(nu, 0);
+    std::vector<float> damp0(nu, 0.f);
     parallel_items<NoScratch>(nu, 256, [&](NoScratch &, int64_t q) {
-        const PullTile &ti = tiles[unit_tile[q]];
-        const int64_t u = q - T.tile_unit_off[unit_tile[q]];
+        const PullTile &ti = tiles[q / team_warps];
+        const int64_t u = q % team_warps;
+        if (32 * u >= ti.nm) return;
+        lanes[q] = (uint8_t)std::min<int64_t>(32, ti.nm - 32 * u);
         int nc = 0;
-        uint32_t na = 0;
-        for (int l = 0; l < 32 && 32 * u + l < ti.nm; l++) {
+        bool first = true;
+        for (int l = 0; l < lanes[q]; l++) {
             const int d = P.deg[ti.mass_off + 32 * u + l];
             if (d == 255) {
                 heavy[q] = 1;
@@ -1019,84 +1011,65 @@ std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, const 
             }
             nc = std::max(nc, d);
             for (int j = 0; j < d; j++) {
-                const uint32_t ends = P.ent_ends[ti.ent_off + (code_of(ti, u, l, j) & 0x7fff)];
-                if (((ends >> 24) & 3u) >= 2) na++;
+                const int64_t sj = P.ent_spring[ti.ent_off + (code_of(ti, u, l, j) & 0x7fff)];
+                const float c = sp.damping ? (float)sp.damping[sj] : 0.f;
+                if (first) {
+                    damp0[q] = c;
+                    first = false;
+                } else if (std::memcmp(&c, &damp0[q], 4) != 0) {
+                    damp[q] = 1;
+                }
             }
         }
-        ncols[q] = (uint16_t)nc;
-        nact[q] = na;
+        nq[q] = (uint16_t)((nc + 3) / 4);
     });
     for (int64_t q = 0; q < nu; q++)
         if (heavy[q]) return "a mass of degree above the heavy threshold (the pull form has no warp-cooperative sums)";
-    std::vector<uint64_t> ell_off(nu + 1, 0), act_off(nu + 1, 0);
-    for (int64_t q = 0; q < nu; q++) {
-        ell_off[q + 1] = ell_off[q] + pull_block_bytes(ncols[q]);
-        act_off[q + 1] = act_off[q] + kPullActHeader + nact[q];
-    }
-    if (ell_off[nu] / 128 > UINT32_MAX || act_off[nu] > UINT32_MAX) return "pull tables exceed their 32-bit offsets";
-    T.units.resize(nu);
-    T.ell.assign(std::max<uint64_t>(ell_off[nu], 128), 0);
-    T.act.assign(4 * std::max<uint64_t>(act_off[nu], 1), 0.f);
+    std::vector<uint64_t> off(nu + 1, 0);
+    for (int64_t q = 0; q < nu; q++) off[q + 1] = off[q] + (uint64_t)nq[q] * pull_quad_bytes(damp[q] != 0);
+    if (off[nu] / 128 > UINT32_MAX) return "pull tables exceed their 32-bit offsets";
+    T.units.assign(nu, PullUnit{});
+    T.ell.assign(std::max<uint64_t>(off[nu], 128), 0);
     // pass 2: fill
     parallel_items<NoScratch>(nu, 256, [&](NoScratch &, int64_t q) {
-        const PullTile &ti = tiles[unit_tile[q]];
-        const int64_t u = q - T.tile_unit_off[unit_tile[q]];
-        const int nc = ncols[q];
-        uint8_t *blk = T.ell.data() + ell_off[q];
-        uint16_t *words = reinterpret_cast<uint16_t *>(blk);
-        float *kc = reinterpret_cast<float *>(blk + pull_words_bytes(nc));
-        float *rc = kc + 32 * (int64_t)nc;
-        float *dc = rc + 32 * (int64_t)nc;
-        float *rec = T.act.data() + 4 * act_off[q];
-        uint16_t *off = reinterpret_cast<uint16_t *>(rec);
-        float *recs = rec + 4 * kPullActHeader;
-        uint32_t na = 0;
-        bool uniform = true, first = true;
-        float damp0 = 0.f;
-        for (int l = 0; l < 32; l++) {
-            off[l] = (uint16_t)na;
-            if (32 * u + l >= ti.nm) continue;
-            const int64_t self = 32 * u + l;
-            const int d = P.deg[ti.mass_off + self];
+        const PullTile &ti = tiles[q / team_warps];
+        const int64_t u = q % team_warps;
+        PullUnit &pu = T.units[q];
+        pu.ell = (uint32_t)(off[q] / 128);
+        pu.nquads = nq[q];
+        pu.lanes = lanes[q];
+        pu.flags = damp[q] ? PU_DAMP : 0;
+        pu.damping = damp[q] ? 0.f : damp0[q];
+        pu.mass0 = (int32_t)(ti.mass_off + 32 * u);
+        const uint32_t qb = pull_quad_bytes(damp[q] != 0);
+        for (int l = 0; l < lanes[q]; l++) {
+            const int d = P.deg[ti.mass_off + 32 * u + l];
             for (int j = 0; j < d; j++) {
+                uint8_t *blk = T.ell.data() + off[q] + (uint64_t)(j / 4) * qb;
+                const int c = j % 4;
                 const uint16_t code = code_of(ti, u, l, j);
-                const int64_t e = ti.ent_off + (code & 0x7fff);
-                const uint32_t ends = P.ent_ends[e];
+                const uint32_t e_local = code & 0x7fffu;
+                const uint32_t ends = P.ent_ends[ti.ent_off + e_local];
                 const uint32_t ls = ends & 0xfffu, rs = (ends >> 12) & 0xfffu, ty = (ends >> 24) & 3u;
                 const uint32_t nbr = (code & 0x8000) ? rs : ls;
-                const int64_t j_sp = P.ent_spring[e];
-                words[32 * j + l] = (uint16_t)(nbr | (ty >= 2 ? 0x8000u : 0u));
-                kc[32 * j + l] = (float)sp.k[j_sp];
-                rc[32 * j + l] = (float)sp.rest[j_sp];
-                const float c = sp.damping ? (float)sp.damping[j_sp] : 0.f;
-                dc[32 * j + l] = c;
-                if (first) {
-                    damp0 = c;
-                    first = false;
-                } else if (std::memcmp(&c, &damp0, 4) != 0) {
-                    uniform = false;
+                const int64_t sj = P.ent_spring[ti.ent_off + e_local];
+                const bool act = ty >= 2;
+                const uint16_t w = (uint16_t)((nbr * (uint32_t)rec_f4) | PW_VALID | (act ? PW_ACT : 0u));
+                std::memcpy(blk + 8 * l + 2 * c, &w, 2);
+                const float kf = (float)sp.k[sj];
+                std::memcpy(blk + 256 + 16 * l + 4 * c, &kf, 4);
+                if (act) {
+                    std::memcpy(blk + 768 + 16 * l + 4 * c, &e_local, 4);
+                } else {
+                    const float rf = (float)sp.rest[sj];
+                    std::memcpy(blk + 768 + 16 * l + 4 * c, &rf, 4);
                 }
-                if (ty >= 2) {
-                    const double om = sp.omega ? sp.omega[j_sp] : 0.0;
-                    const double am = sp.amp ? sp.amp[j_sp] : 0.2;
-                    const double ph = sp.phase ? sp.phase[j_sp] : 0.0;
-                    float *r = recs + 4 * (int64_t)na;
-                    r[0] = (float)(om / kTwoPi);
-                    r[1] = (float)(ty == 2 ? -am : am);
-                    r[2] = (float)(ph / kTwoPi);
-                    r[3] = 0.f;
-                    na++;
+                if (damp[q]) {
+                    const float cf = sp.damping ? (float)sp.damping[sj] : 0.f;
+                    std::memcpy(blk + 1280 + 16 * l + 4 * c, &cf, 4);
                 }
-                (void)self;
             }
         }
-        off[32] = (uint16_t)na;
-        PullUnit &pu = T.units[q];
-        pu.ell = (uint32_t)(ell_off[q] / 128);
-        pu.ncols = (uint16_t)nc;
-        pu.flags = uniform ? 0 : PU_DAMP;
-        pu.damping = uniform ? damp0 : 0.f;
-        pu.act = (uint32_t)act_off[q];
     });
     return "";
 } catch (const std::bad_alloc &) {

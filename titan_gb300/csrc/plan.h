@@ -112,28 +112,27 @@ struct ResPlan {
 void build_resident(const PlanInput &in, const Plan &P, int max_masses, int bin_cap, ResPlan &R);
 
 // Spring tables of the pull form (pull_layout.h), derived from a tile plan
-// for the tiles the per-step kernel runs.  A tile's units are 32 consecutive
-// tile masses each; lane l of unit u lists the springs of tile mass 32u + l
-// in its incidence order (ascending spring index), each as the other end's
-// tile-local slot and the spring's k, rest, damping and actuation, in the
-// FP32 forms' rounding.
+// for the tiles the per-step kernel runs: team_warps unit slots per tile;
+// lane l of unit u lists the springs of tile mass 32u + l in its incidence
+// order (ascending spring index), each as the other end's state record
+// (float4 index: tile-local slot * rec_f4) and the spring's k, rest and
+// damping in the FP32 forms' rounding; an actuated spring carries its slab
+// entry index in place of rest.
 struct PullTile {
     int64_t mass_off = 0, ent_off = 0, warp_off = 0;
     int32_t nm = 0;
 };
 struct PullSprings {
     const double *k = nullptr, *rest = nullptr, *damping = nullptr;
-    const int32_t *type = nullptr;  // null: all passive
-    const double *omega = nullptr, *amp = nullptr, *phase = nullptr;  // null: 0, 0.2, 0
 };
 struct PullTables {
-    std::vector<int32_t> tile_unit_off;  // per tile: its first unit
-    std::vector<PullUnit> units;
-    std::vector<uint8_t> ell;            // unit blocks
-    std::vector<float> act;              // 4 floats per 16-byte record (headers and records)
+    int team_warps = 0;
+    std::vector<PullUnit> units;  // ntiles * team_warps
+    std::vector<uint8_t> ell;     // quad blocks
 };
 // Returns "" on success, else why the pull form cannot run the plan (a heavy
 // mass, whose incidence list the plan keeps apart); throws nothing.
-std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, const PullSprings &sp, PullTables &out);
+std::string build_pull(const Plan &P, const std::vector<PullTile> &tiles, int team_warps, int rec_f4,
+                       const PullSprings &sp, PullTables &out);
 
 }  // namespace tg

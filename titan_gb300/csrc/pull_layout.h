@@ -8,21 +8,24 @@
 // do not), so the sums equal the slab forms' bit for bit.
 //
 // Tables, per unit of 32 consecutive tile masses (lane l = tile-local mass
-// 32 u + l), built from the tile plan:
-//   unit block (128-byte aligned, ncols = the unit's largest degree):
-//     words    uint16 [ncols][32]  neighbour's tile-local slot | 0x8000 when
-//                                  the spring is actuated (padded to 128 B)
-//     k        float  [ncols][32]
-//     rest     float  [ncols][32]
-//     damping  float  [ncols][32]  read only when the unit's damping is not
-//                                  uniform (PU_DAMP), else PullUnit::damping
-//   column j of lane l is that mass's j-th spring; lanes whose degree is at
-//   most j have no column j (never read).
-//   actuation block (16-byte records, at PullUnit::act): a header of
-//     kPullActHeader records holding uint16 off[33] -- lane l's records are
-//     [off[l], off[l+1]) after the header -- then records {nu = omega / 2 pi,
-//     +-amp (minus for contract-then-expand), phi = phase / 2 pi, 0} in each
-//     lane's incidence order.
+// 32 u + l), built from the tile plan.  Every tile has team_warps unit slots
+// (unit u of tile t is units[t * team_warps + u]; slots past the tile's
+// masses have lanes == 0), so a warp finds its next unit without reading the
+// tile record first.  A unit's columns (lane l's j-th spring in its
+// incidence order) come in quads of four columns, each quad a 128-byte
+// aligned block of
+//     words    uint16 [32 lanes][4]  neighbour's state record as a float4
+//                                    index (tile-local slot * record
+//                                    float4s) | PW_VALID | PW_ACT
+//     k        float  [32][4]
+//     rest     float  [32][4]        for an actuated spring: the bits of its
+//                                    slab entry index (< the tile's nact),
+//                                    whose actuation record {nu, +-amp, phi,
+//                                    rest} the producer stages with the
+//                                    tile's states
+//     damping  float  [32][4]        only when PU_DAMP (else the unit's
+//                                    uniform PullUnit::damping)
+// Columns past a lane's degree are padding (word 0).
 #pragma once
 
 #include <cstdint>
@@ -38,20 +41,19 @@
 namespace tg {
 
 struct PullUnit {
-    uint32_t ell;     // unit block offset in 128-byte units
-    uint16_t ncols;   // columns (largest degree among the unit's masses)
-    uint16_t flags;   // PU_DAMP: per-column damping
+    uint32_t ell;     // first quad, in 128-byte units
+    uint16_t nquads;  // quads of columns (the unit's largest degree, rounded up to 4, / 4)
+    uint8_t lanes;    // masses in the unit (0: no unit in this slot)
+    uint8_t flags;    // PU_DAMP: per-column damping
     float damping;    // the unit's damping when uniform
-    uint32_t act;     // actuation header offset in 16-byte records
+    int32_t mass0;    // tiled index of lane 0's mass
 };
 static_assert(sizeof(PullUnit) == 16, "PullUnit is loaded as one 16-byte vector");
 
 enum { PU_DAMP = 1 };
-constexpr int kPullActHeader = 5;  // 33 uint16 lane offsets in 16-byte records
+enum : uint32_t { PW_VALID = 0x4000u, PW_ACT = 0x8000u, PW_SLOT = 0x3fffu };
 
-// bytes of the words array of a unit block with ncols columns
-TG_PULL_HD inline constexpr uint32_t pull_words_bytes(int ncols) { return (uint32_t)((ncols * 64 + 127) & ~127); }
-// bytes of a whole unit block
-TG_PULL_HD inline constexpr uint64_t pull_block_bytes(int ncols) { return pull_words_bytes(ncols) + 3ull * (uint64_t)ncols * 128; }
+// bytes of one quad block
+TG_PULL_HD inline constexpr uint32_t pull_quad_bytes(bool damp) { return damp ? 1792u : 1280u; }
 
 }  // namespace tg
