@@ -341,6 +341,46 @@ int titan_gb300_diagnostics_noalloc(const double *pos, const double *vel, const 
                                     const double *rest, int64_t ns, double g_mag, double *out,
                                     void *stream);
 
+/* ---- device-resident request server ---------------------------------------
+ * Extension with no counterpart in the reference, which runs one scene per
+ * process on a host thread that launches two kernels per step
+ * (src/sim.cu:1389-1428, 1503-1617).  A server is one persistent kernel
+ * (cooperative launch, one CTA per SM) that steps many started scenes at
+ * once: each submitted scene takes a slot, is admitted at the next step
+ * boundary and stepped nsteps times with the per-tile kernel's arithmetic
+ * (bit-identical to the scene's own step(), whatever else is running), and
+ * its slot is freed when its steps are done.  Submissions go through a ring
+ * in page-locked host memory that the kernel reads between steps; finished
+ * requests are reported in page-locked memory the host polls.  The kernel
+ * leaves after a second without work and is launched again by the next
+ * submit or poll; every wait in it is bounded.
+ *   create: max_slots scenes at once (1 to 16384); tile_smem_bytes of
+ *     shared memory for one tile (0: 96 KiB; scenes whose tiles need more
+ *     are refused -- plan them with smaller tiles).
+ *   submit: the scene must be started (start()) on the server's device and
+ *     precision, with symplectic Euler and resident tiles and bins off
+ *     (set_resident 0).  Its queued work is waited for; until poll reports
+ *     the request done, the scene's own stepping, transfers and parameter
+ *     changes return TITAN_GB300_ESTATE.  TITAN_GB300_EBUSY: no free slot.
+ *     *ticket identifies the request.
+ *   poll: TITAN_GB300_OK once the request is done (the scene's clock and
+ *     step count have advanced by nsteps and it is usable again),
+ *     TITAN_GB300_EBUSY while it runs, TITAN_GB300_ETIMEOUT if the kernel's
+ *     bounded waits gave up (the server is then unusable).
+ *   info: out[0] occupied slots, [1] free slots, [2] kernel launches so far,
+ *     [3] the kernel's last status (1 running, 2 stopped, 3 left idle, 4
+ *     timed out), [4] CTAs, [5] dynamic shared memory per CTA.
+ *   destroy: a stop word ends the kernel at its next step boundary; scenes
+ *     still in flight are released with an undefined state. */
+typedef struct titan_gb300_server titan_gb300_server;
+int titan_gb300_server_create(titan_gb300_server **out, int device, int precision, int max_slots,
+                              int64_t tile_smem_bytes);
+int titan_gb300_server_submit(titan_gb300_server *srv, titan_gb300_sim *sim, int64_t nsteps, int64_t *ticket);
+int titan_gb300_server_poll(titan_gb300_server *srv, int64_t ticket);
+int titan_gb300_server_info(const titan_gb300_server *srv, int64_t out[6]);
+const char *titan_gb300_server_last_error(const titan_gb300_server *srv);
+void titan_gb300_server_destroy(titan_gb300_server *srv);
+
 /* CUDA stream (cudaStream_t) the handle queues work on. */
 void *titan_gb300_stream(titan_gb300_sim *sim);
 

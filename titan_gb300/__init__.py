@@ -16,8 +16,8 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["FP64", "FP32", "FP32C", "TitanError", "Sim", "lattice", "lattice_springs", "lib", "pinned_empty",
-           "library_path"]
+__all__ = ["FP64", "FP32", "FP32C", "TitanError", "Sim", "Server", "lattice", "lattice_springs", "lib",
+           "pinned_empty", "library_path"]
 
 FP64, FP32, FP32C = 0, 1, 2
 EULER, VERLET, RK2 = 0, 1, 2
@@ -93,6 +93,13 @@ _SIGS = {
     "titan_gb300_lattice_springs": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "titan_gb300_lattice": (ctypes.c_int, [_D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _I32, _I32, _D]),
     "titan_gb300_version": (ctypes.c_char_p, []),
+    "titan_gb300_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int64]),
+    "titan_gb300_server_submit": (ctypes.c_int, [_P, _P, ctypes.c_int64, _I64]),
+    "titan_gb300_server_poll": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "titan_gb300_server_info": (ctypes.c_int, [_P, _I64]),
+    "titan_gb300_server_last_error": (ctypes.c_char_p, [_P]),
+    "titan_gb300_server_destroy": (None, [_P]),
     "titan_gb300_stl_inside": (ctypes.c_int, [ctypes.c_int, _D, ctypes.c_int64, _D, ctypes.c_int64, ctypes.c_int,
                                               ctypes.c_uint64, _U8]),
 }
@@ -474,6 +481,76 @@ class Sim:
         keys = ["masses", "springs", "tiles", "entries", "halo", "inc_words", "heavy", "smem_bytes", "threads",
                 "algorithmic_bytes_per_step", "implementation_bytes_per_step", "actuated_entries"]
         return {k: int(v) for k, v in zip(keys, out)}
+
+
+class Server:
+    """Device-resident request server (titan_gb300_server_*): one persistent
+    kernel steps every submitted Sim (started, symplectic Euler, resident
+    tiles and bins off: set_resident(0)) until its steps are done; each
+    result is bit-identical to the Sim's own step()."""
+
+    def __init__(self, precision: int = FP32C, device: int = 0, max_slots: int = 4096, tile_smem_bytes: int = 0):
+        self._L = lib()
+        h = _P()
+        rc = self._L.titan_gb300_server_create(ctypes.byref(h), device, precision, max_slots, tile_smem_bytes)
+        if rc:
+            raise TitanError(rc, "server_create")
+        self._h = h
+        self.precision = precision
+        self.max_slots = max_slots
+
+    def _check(self, rc, what):
+        if rc:
+            msg = self._L.titan_gb300_server_last_error(self._h)
+            raise TitanError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def submit(self, sim: "Sim", nsteps: int):
+        """Queue nsteps steps of sim; returns a ticket, or None when no slot is free."""
+        t = ctypes.c_int64(0)
+        rc = self._L.titan_gb300_server_submit(self._h, sim._h, int(nsteps), ctypes.byref(t))
+        if rc == 8:  # TITAN_GB300_EBUSY
+            return None
+        self._check(rc, "server_submit")
+        return int(t.value)
+
+    def poll(self, ticket: int) -> bool:
+        """True once the request is done (its Sim is usable again)."""
+        rc = self._L.titan_gb300_server_poll(self._h, int(ticket))
+        if rc == 8:
+            return False
+        self._check(rc, "server_poll")
+        return True
+
+    def wait(self, ticket: int, timeout_s: float = 600.0, sleep_s: float = 50e-6) -> None:
+        import time
+        t0 = time.perf_counter()
+        while not self.poll(ticket):
+            if time.perf_counter() - t0 > timeout_s:
+                raise TitanError(6, f"request {ticket} not done after {timeout_s} s")
+            time.sleep(sleep_s)
+
+    def info(self) -> dict:
+        out = np.zeros(6, np.int64)
+        self._check(self._L.titan_gb300_server_info(self._h, _ptr(out, ctypes.c_int64)), "server_info")
+        keys = ("busy_slots", "free_slots", "launches", "status", "ctas", "smem_bytes")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.titan_gb300_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def stl_inside(tri, pts, num_rays: int = 5, seed: int = 1, device: int = 0) -> np.ndarray:

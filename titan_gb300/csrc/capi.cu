@@ -128,6 +128,7 @@ struct titan_gb300_sim {
     int kernel_req = 0;   // 0 auto, 1 per-tile kernel, 3 per-tile with async staging, 4 warp-specialised, 6 pull
     bool use_async = false;
     bool use_ws = false;
+    bool serving = false;  // handed to a request server (server.cu)
     bool use_pull = false;
     tg::PullTables pull;  // host copy of the pull form's spring tables
     std::vector<tg::PullTile> pull_tiles;
@@ -1117,6 +1118,40 @@ int check_kernel_error(titan_gb300_sim *s) {
 
 }  // namespace
 
+namespace tg {
+
+int serve_begin(titan_gb300_sim *s, int device, int precision, size_t tile_smem, ServeScene &v, std::string &why) {
+    if (!s->started) return why = "the scene has not started", TITAN_GB300_ESTATE;
+    if (s->serving) return why = "the scene is already with a server", TITAN_GB300_ESTATE;
+    if (s->device != device || s->prec != precision)
+        return why = "the scene's device or precision differs from the server's", TITAN_GB300_EINVAL;
+    if (s->integrator != INTEG_EULER) return why = "the server steps symplectic Euler only", TITAN_GB300_EINVAL;
+    if (s->use_res || s->use_rtiles || s->args.ntiles <= 0)
+        return why = "start the scene with resident tiles and bins off (set_resident 0)", TITAN_GB300_EINVAL;
+    size_t need = 0;
+    for (const TileInfo &ti : tile_infos(s->plan))
+        need = std::max(need, tile_smem_bytes(s->prec, ti.nm + ti.nh, ti.ne + 1, ti.nheavy));
+    if (need > tile_smem)
+        return why = "a tile needs more shared memory than the server has (plan smaller tiles)", TITAN_GB300_ELIMIT;
+    if (!ensure_device(s)) return why = "cudaSetDevice failed", TITAN_GB300_ECUDA;
+    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return why = std::string("scene stream: ") + cudaGetErrorString(e), TITAN_GB300_ECUDA;
+    s->serving = true;
+    v.args = &s->args;
+    v.parity = s->parity;
+    return TITAN_GB300_OK;
+}
+
+void serve_end(titan_gb300_sim *s, int64_t nsteps) {
+    s->serving = false;
+    if (nsteps <= 0) return;
+    s->parity ^= (int)(nsteps & 1);
+    for (int64_t i = 0; i < nsteps; i++) s->T = s->T + s->dt;  // src/sim.cu:1590
+    s->steps += nsteps;
+}
+
+}  // namespace tg
+
 // Status of a C++ exception that reached an entry point (a host allocation
 // that failed, or a library error): the C ABI throws nothing, and the
 // message goes to the handle when there is one.
@@ -1446,6 +1481,7 @@ int titan_gb300_set_local_constraints(titan_gb300_sim *s, const int64_t *mass_pt
 
 int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double offset, double fk, double fs) try {
     if (!s || !normal) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if ((int)s->planes.size() >= tg::kMaxPlanes) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global planes");
     double nn = norm3(normal);
     if (!(nn > 0)) return s->fail(TITAN_GB300_EINVAL, "zero plane normal");
@@ -1458,6 +1494,7 @@ int titan_gb300_add_plane(titan_gb300_sim *s, const double normal[3], double off
 
 int titan_gb300_add_ball(titan_gb300_sim *s, const double center[3], double radius) try {
     if (!s || !center) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if ((int)s->balls.size() >= tg::kMaxBalls) return s->fail(TITAN_GB300_ELIMIT, "at most 16 global balls");
     s->balls.push_back({center[0], center[1], center[2], radius});
     if (s->started) return upload_params(s);
@@ -1468,6 +1505,7 @@ int titan_gb300_add_ball(titan_gb300_sim *s, const double center[3], double radi
 
 int titan_gb300_clear_constraints(titan_gb300_sim *s) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     s->planes.clear();
     s->balls.clear();
     if (s->started) return upload_params(s);
@@ -1478,6 +1516,7 @@ int titan_gb300_clear_constraints(titan_gb300_sim *s) try {
 
 int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (kind < tg::INTEG_EULER || kind > tg::INTEG_RK2)
         return s->fail(TITAN_GB300_EINVAL, "integrator must be 0 (Euler), 1 (Verlet) or 2 (RK2)");
     if (kind == s->integrator) return TITAN_GB300_OK;
@@ -1510,6 +1549,7 @@ int titan_gb300_set_integrator(titan_gb300_sim *s, int kind) try {
 
 int titan_gb300_set_time_step(titan_gb300_sim *s, double dt) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!(dt > 0)) return s->fail(TITAN_GB300_EINVAL, "Cannot set time step to negative or zero value.");
     s->dt = dt;
     if (s->started) {
@@ -1525,6 +1565,7 @@ double titan_gb300_get_time_step(const titan_gb300_sim *s) { return s ? s->dt : 
 
 int titan_gb300_set_global_acc(titan_gb300_sim *s, const double g[3]) try {
     if (!s || !g) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     for (int c = 0; c < 3; c++) s->g[c] = g[c];
     if (s->started) return upload_params(s);
     return TITAN_GB300_OK;
@@ -1585,6 +1626,7 @@ int titan_gb300_start(titan_gb300_sim *s, int tile_masses) try {
 
 int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (nsteps < 0) return s->fail(TITAN_GB300_EINVAL, "negative step count");
     if (nsteps == 0) return TITAN_GB300_OK;
@@ -1658,6 +1700,7 @@ int titan_gb300_step(titan_gb300_sim *s, int64_t nsteps) try {
 
 int titan_gb300_prepare_steps(titan_gb300_sim *s, int64_t nsteps) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (nsteps < 0) return s->fail(TITAN_GB300_EINVAL, "negative step count");
     if (s->args.ntiles == 0 || nsteps <= 1) return TITAN_GB300_OK;
@@ -1715,6 +1758,7 @@ int titan_gb300_wait(titan_gb300_sim *s, double timeout_ms) try {
 
 int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_device) try {
     if (!s || !out) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
     tg::XferArgs x{};
@@ -1742,6 +1786,7 @@ int titan_gb300_export_vertices(titan_gb300_sim *s, float *out, int out_on_devic
 
 int titan_gb300_export_indices(titan_gb300_sim *s, uint32_t *out, int out_on_device) try {
     if (!s || !out) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     std::vector<uint32_t> idx(2 * (size_t)s->ns, 0);
     for (int64_t j = 0; j < s->ns; j++) {
         const int32_t l = s->left[j], r = s->right[j];
@@ -1781,6 +1826,7 @@ void titan_gb300_host_free(void *p) {
 
 int titan_gb300_set_time(titan_gb300_sim *s, double T) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     s->T = T;
     if (!s->started) return TITAN_GB300_OK;
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
@@ -1793,6 +1839,7 @@ int64_t titan_gb300_steps(const titan_gb300_sim *s) { return s ? s->steps : 0; }
 int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx, double *pos, double *vel,
                            double *acc, double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (count < 0 || count > s->n) return s->fail(TITAN_GB300_EINVAL, "bad count");
     if (idx)
@@ -1841,6 +1888,7 @@ int titan_gb300_get_masses(titan_gb300_sim *s, int64_t count, const int64_t *idx
 
 int titan_gb300_get_state(titan_gb300_sim *s, double *pos, double *vel, double *acc, double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     return titan_gb300_get_masses(s, s->n, nullptr, pos, vel, acc, T);
 } catch (...) {
     return host_exception(s);
@@ -1850,6 +1898,7 @@ int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t 
                                const double *vel, const double *m, const double *ext, const uint8_t *fixed,
                                const double *drag, const double *T) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!idx) count = s->n;
     if (count < 0 || count > s->n) return s->fail(TITAN_GB300_EINVAL, "bad count");
@@ -1949,6 +1998,7 @@ int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64
                                   const double *rest, const double *damping, const int32_t *type,
                                   const double *omega, const double *amp, const double *phase) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!idx) count = s->ns;
     if (count < 0 || count > s->ns) return s->fail(TITAN_GB300_EINVAL, "bad count");
     bool replan = false;
@@ -2010,6 +2060,7 @@ int titan_gb300_set_spring_params(titan_gb300_sim *s, int64_t count, const int64
 
 int titan_gb300_diagnostics(titan_gb300_sim *s, double g_mag, double energy[4], double momentum[6]) try {
     if (!s) return TITAN_GB300_EINVAL;
+    if (s->serving) return s->fail(TITAN_GB300_ESTATE, "the scene is being stepped by a request server");
     if (!s->started) return s->fail(TITAN_GB300_ESTATE, "The simulation has not started.");
     if (!ensure_device(s)) return s->fail(TITAN_GB300_ECUDA, "cudaSetDevice failed");
     cudaError_t e = cudaSuccess;

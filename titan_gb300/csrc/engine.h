@@ -21,7 +21,10 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "pull_layout.h"
+#include "titan_gb300.h"
 
 namespace tg {
 
@@ -249,5 +252,20 @@ cudaError_t launch_gather(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_export_f32(int precision, const XferArgs &a, float *out, cudaStream_t s);
 cudaError_t launch_scatter(int precision, const XferArgs &a, cudaStream_t s);
 cudaError_t launch_diag(int precision, const DiagArgs &a, cudaStream_t s);
+
+// A started scene handed to the request server (server.cu): its step
+// arguments and step parity.  serve_begin checks that the server can step
+// it (same device and precision, symplectic Euler, every tile on the
+// per-step kernels, tiles within tile_smem bytes of shared memory), waits for
+// the scene's own queued work and marks it busy (its own stepping, transfers
+// and parameter changes are refused until serve_end); serve_end advances the
+// scene's host-side clock and step count by nsteps (nsteps < 0: abandoned,
+// the scene's state is then undefined) and releases it.
+struct ServeScene {
+    const StepArgs *args;
+    int parity;
+};
+int serve_begin(titan_gb300_sim *s, int device, int precision, size_t tile_smem, ServeScene &v, std::string &why);
+void serve_end(titan_gb300_sim *s, int64_t nsteps);
 
 }  // namespace tg

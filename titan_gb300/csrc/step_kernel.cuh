@@ -58,13 +58,18 @@ __device__ __forceinline__ void copy_record(uint8_t *dst, const uint8_t *src) {
         reinterpret_cast<float4 *>(dst)[v] = __ldg(reinterpret_cast<const float4 *>(src) + v);
 }
 
-template <int PREC, int LBT, int LBM, int INTEG>
-__global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int write_acc) {
+// One step of one tile by the whole CTA (phases A, B, C above) in the
+// dynamic shared memory smem (tile_smem_bytes).  first_tile: this CTA
+// advances the scene's time record.  Callers synchronise the CTA before
+// reusing smem.  L2ONLY: the state and time records are read around L1 (a
+// persistent kernel in which other CTAs wrote them since this SM may have
+// cached them); a kernel launched per step reads them through L1.
+template <int PREC, int LBM, int INTEG, bool L2ONLY = false>
+__device__ __forceinline__ void tile_step(const StepArgs &a, const TileInfo &ti, uint8_t *smem, int parity,
+                                          int write_acc, bool first_tile) {
     using R = typename Real<PREC>::T;
     constexpr int kRec = rec_bytes<PREC>();
     constexpr int kSlot = Slot<PREC>::kBytes;
-    extern __shared__ __align__(16) uint8_t smem[];
-    const TileInfo ti = a.tiles[blockIdx.x];
     const int S = ti.nm + ti.nh, E = ti.ne;
     uint8_t *st = smem;                                   // S state records
     uint8_t *slots = smem + align16((int64_t)S * kRec);   // E force slots
@@ -73,8 +78,8 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
     void *out = parity ? a.state0 : a.state1;
     const int64_t np = a.npad;
     const DevParams *prm = a.prm;
-    const StepTime t = step_time(a.tbuf[parity]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->launch_dt;
+    const StepTime t = step_time(L2ONLY ? __ldcg(a.tbuf + parity) : a.tbuf[parity]);
+    if (first_tile && threadIdx.x == 0) a.tbuf[parity ^ 1] = t.T + prm->launch_dt;
 
     // phase-C inputs of this thread's own mass, issued first
     const int i_own = threadIdx.x;
@@ -99,10 +104,16 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
         if (i1 < S) g1 = i1 < ti.nm ? (int64_t)ti.mass_off + i1 : (int64_t)__ldg(a.halo + ti.halo_off + i1 - ti.nm);
         float4 v0[kRec / 16], v1[kRec / 16];
 #pragma unroll
-        for (int v = 0; v < kRec / 16; v++) v0[v] = __ldg(reinterpret_cast<const float4 *>(in + g0 * kRec) + v);
+        for (int v = 0; v < kRec / 16; v++) {
+            const float4 *p = reinterpret_cast<const float4 *>(in + g0 * kRec) + v;
+            v0[v] = L2ONLY ? __ldcg(p) : __ldg(p);
+        }
         if (i1 < S) {
 #pragma unroll
-            for (int v = 0; v < kRec / 16; v++) v1[v] = __ldg(reinterpret_cast<const float4 *>(in + g1 * kRec) + v);
+            for (int v = 0; v < kRec / 16; v++) {
+                const float4 *p = reinterpret_cast<const float4 *>(in + g1 * kRec) + v;
+                v1[v] = L2ONLY ? __ldcg(p) : __ldg(p);
+            }
         }
 #pragma unroll
         for (int v = 0; v < kRec / 16; v++) reinterpret_cast<float4 *>(st + (int64_t)i0 * kRec)[v] = v0[v];
@@ -195,6 +206,13 @@ __global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int w
         St<PREC> s = load_state_smem<PREC>(st, i);
         integrate<PREC, INTEG>(a, ti, g, fl, m, F0, F1, F2, s, out, g, write_acc, np, prm);
     }
+}
+
+template <int PREC, int LBT, int LBM, int INTEG>
+__global__ void __launch_bounds__(LBT, LBM) k_step(StepArgs a, int parity, int write_acc) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const TileInfo ti = a.tiles[blockIdx.x];
+    tile_step<PREC, LBM, INTEG>(a, ti, smem, parity, write_acc, blockIdx.x == 0);
 }
 
 }  // namespace
