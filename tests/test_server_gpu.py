@@ -114,7 +114,8 @@ def test_server_fp64_bitwise_vs_oracle_and_refusals():
         for k, v in (("pos", o.pos), ("vel", o.vel), ("acc", o.acc), ("T", o.T)):
             assert np.array_equal(st[k], v), k
         # scenes the server cannot step are refused
-        r = wl.make_sim(sc, tg.FP64)  # automatic: resident tiles
+        r = wl.make_sim(sc, tg.FP64, 128, resident=(2, 0, 0))  # one halo-free tile, run resident
+        assert r.resident_info()["active"] == 2
         with pytest.raises(tg.TitanError, match="EINVAL"):
             srv.submit(r, 10)
         f = wl.make_sim(sc, tg.FP32C, 32, kernel=1, resident=(0, 0, 0))

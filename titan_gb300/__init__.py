@@ -23,7 +23,7 @@ FP64, FP32, FP32C = 0, 1, 2
 EULER, VERLET, RK2 = 0, 1, 2
 PRECISION_NAMES = {FP64: "f64", FP32: "f32", FP32C: "f32c"}
 
-_ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ELIMIT", 5: "ESTATE", 6: "ETIMEOUT", 7: "EBUDGET"}
+_ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ELIMIT", 5: "ESTATE", 6: "ETIMEOUT", 7: "EBUDGET", 8: "EBUSY"}
 
 _LIB = None
 
