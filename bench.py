@@ -29,6 +29,8 @@ import sys
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -65,7 +67,15 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-max-masses", type=int, default=200000)
     p.add_argument("--serve-small-masses", type=int, default=50000,
-                   help="requests below this many masses run the per-tile kernel (0: all automatic)")
+                   help="streams engine: requests below this many masses run the per-tile kernel (0: all automatic)")
+    p.add_argument("--serve-rates", default="100,300,1000,3000,5000",
+                   help="comma-separated arrival rates (req/s) to sweep, one JSON line each")
+    p.add_argument("--serve-engine", default="device", choices=["device", "streams"],
+                   help="device: the persistent request-server kernel; streams: one engine per request on its "
+                        "own CUDA stream")
+    p.add_argument("--serve-bodies", type=int, default=0,
+                   help="instead of the rate sweep: this many single-body robot rollouts (3-12 masses per side, "
+                        "5000 steps) submitted at once")
     p.add_argument("--ref-gpu-steps", type=int, default=50,
                    help="steps of the reference's own CUDA kernels timed beside ours (0: skip)")
     return p.parse_args()
@@ -586,10 +596,13 @@ def run_precision_study(a, local):
 
 
 def run_serving(a, local):
-    """Rollout serving: requests with Poisson arrivals (--serve-rate per s),
-    masses log-uniform in [27, --serve-max-masses] (cube side =
-    round(cbrt)), horizon U[100, 5000] steps, 120 GB HBM budget; latency from
-    arrival to the final positions on the host."""
+    """Rollout serving.  Rate sweep: requests with Poisson arrivals at each
+    rate of --serve-rates, masses log-uniform in [27, --serve-max-masses]
+    (cube side = round(cbrt)), horizon U[100, 5000] steps, 120 GB HBM budget
+    (the same requests at every rate; only arrival times scale).  Bodies:
+    --serve-bodies single-body robots (3-12 masses per side, 5% of springs
+    removed, 30% actuated) submitted together for 5000 steps.  Latency runs
+    from arrival to the final positions on the host; one JSON line per rate."""
     import torch
 
     import titan_gb300 as tg
@@ -598,22 +611,42 @@ def run_serving(a, local):
 
     torch.cuda.set_device(local)
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
-    reqs = wl.request_stream(a.serve_requests, a.serve_rate, mass_range=(27, a.serve_max_masses))
+    if a.serve_engine == "device":
+        srv = serving.DeviceRolloutServer(prec, device=local)
+        engine = "device-resident request server (one persistent kernel, per-tile arithmetic, tiles of 128 masses)"
+    else:
+        srv = serving.RolloutServer(prec, device=local, small_masses=a.serve_small_masses)
+        engine = "one engine per request on its own CUDA stream"
+    if a.serve_bodies:
+        rng = np.random.default_rng(11)
+        reqs = [{"id": i, "arrival_s": 0.0, "side": int(rng.integers(3, 13)), "steps": 5000, "seed": 7000 + i}
+                for i in range(a.serve_bodies)]
+        runs = [("bodies", reqs)]
+    else:
+        runs = [(float(r), wl.request_stream(a.serve_requests, float(r), mass_range=(27, a.serve_max_masses)))
+                for r in a.serve_rates.split(",")]
     # scenes built before the clock starts (request payloads arrive ready)
-    scenes = {r["id"]: wl.rollout_request(r["side"], r["seed"]) for r in reqs}
-    srv = serving.RolloutServer(prec, device=local, small_masses=a.serve_small_masses)
-    # warm-up: one request per design, so that the served run measures
-    # steady state (plans, engines and graphs exist)
+    scenes = {}
+    for _, reqs in runs:
+        for r in reqs:
+            scenes.setdefault((r["side"], r["seed"]), None)
+    for key in scenes:
+        scenes[key] = wl.rollout_request(*key)
+    scene_of = lambda r: scenes[(r["side"], r["seed"])]
+    # warm-up: one short request per design, so that the served runs measure
+    # steady state (plans and pooled engines exist)
     warm = {}
-    for r in reqs:
-        warm.setdefault(r["side"], dict(r, arrival_s=0.0, steps=100))
-    srv.run(list(warm.values()), scene_of=lambda r: scenes[r["id"]])
-    recs, stats = srv.run(reqs, scene_of=lambda r: scenes[r["id"]])
+    for _, reqs in runs:
+        for r in reqs:
+            warm.setdefault(r["side"], dict(r, arrival_s=0.0, steps=100))
+    srv.run(list(warm.values()), scene_of=scene_of)
+    for rate, reqs in runs:
+        recs, stats = srv.run(reqs, scene_of=scene_of)
+        masses = sum(rec["masses"] for rec in recs.values())
+        print(json.dumps({"workload": "rollout serving", "engine": engine, "requests": len(reqs),
+                          "rate_per_s": rate, "mean_masses": masses / len(recs), "precision": a.precision, **stats,
+                          "unit": UNIT}), flush=True)
     srv.close()
-    masses = sum(rec["masses"] for rec in recs.values())
-    print(json.dumps({"workload": "rollout serving", "requests": len(reqs), "rate_per_s": a.serve_rate,
-                      "mean_masses": masses / len(recs), "precision": a.precision, **stats,
-                      "unit": UNIT}), flush=True)
 
 
 def main():

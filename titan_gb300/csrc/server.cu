@@ -36,6 +36,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "engine.h"
@@ -315,6 +316,7 @@ struct titan_gb300_server {
         uint64_t ticket = 0;
     };
     std::vector<Req> req;  // per slot
+    std::unordered_map<uint64_t, int> slot_of;  // ticket -> slot, requests in flight
     uint64_t next_ticket = 0;
     int64_t launches = 0;
     bool launched = false;
@@ -448,6 +450,7 @@ int titan_gb300_server_submit(titan_gb300_server *s, titan_gb300_sim *sim, int64
     }
     s->free_slots.pop_back();
     s->req[si] = {sim, nsteps, sl.ticket};
+    s->slot_of[sl.ticket] = si;
     const uint64_t head = s->h_host->head;
     s->h_host->ring[head % tg::kRing] = si;
     __atomic_store_n(&s->h_host->head, head + 1, __ATOMIC_RELEASE);
@@ -460,13 +463,13 @@ int titan_gb300_server_submit(titan_gb300_server *s, titan_gb300_sim *sim, int64
 int titan_gb300_server_poll(titan_gb300_server *s, int64_t ticket) try {
     if (!s || ticket < 1) return TITAN_GB300_EINVAL;
     std::lock_guard<std::mutex> lk(s->mu);
-    int si = -1;
-    for (int i = 0; i < s->max_slots && si < 0; i++)
-        if (s->req[i].sim && s->req[i].ticket == (uint64_t)ticket) si = i;
-    if (si < 0) return s->fail(TITAN_GB300_EINVAL, "no such request in flight");
+    const auto it = s->slot_of.find((uint64_t)ticket);
+    if (it == s->slot_of.end()) return s->fail(TITAN_GB300_EINVAL, "no such request in flight");
+    const int si = it->second;
     if (__atomic_load_n(s->h_done + si, __ATOMIC_ACQUIRE) == (uint64_t)ticket) {
         tg::serve_end(s->req[si].sim, s->req[si].nsteps);
         s->req[si] = {};
+        s->slot_of.erase(it);
         s->free_slots.push_back(si);
         return TITAN_GB300_OK;
     }

@@ -33,7 +33,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
-from . import FP32, FP32C, FP64, Sim
+from . import FP32, FP32C, FP64, Server, Sim
 from . import workloads as wl
 
 _SMEM_PER_CTA = 227 * 1024
@@ -146,6 +146,12 @@ class RolloutServer:
             self.bytes_of[side] = float(e.device_bytes())
         return e
 
+    def _launch(self, e, steps):
+        e.step(steps)
+
+    def _done(self, e):
+        return e.poll()
+
     def _release(self, side, e):
         if len(self.pool[side]) < self.pool_per_design:
             self.pool[side].append(e)
@@ -163,6 +169,7 @@ class RolloutServer:
         active = []
         records = {}
         springs_done = 0
+        max_active = 0
         t0 = time.perf_counter()
         try:
             while pending or active:
@@ -187,9 +194,10 @@ class RolloutServer:
                     del pending[idx]
                     del scenes[r["id"]]
                     e = self._engine(r["side"], sc)
-                    e.step(r["steps"])
+                    self._launch(e, r["steps"])
                     self.used += need
                     active.append((r, e, need, time.perf_counter() - t0, sc["left"].size))
+                    max_active = max(max_active, len(active))
                     progressed = True
                 finished, springs = self._poll(active, records, keep_results, t0, time_scale)
                 springs_done += springs
@@ -204,7 +212,8 @@ class RolloutServer:
         lat = np.array([rec["latency_ms"] for rec in records.values()])
         stats = {"requests": len(records), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
                  "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                 "spring_updates_per_s": springs_done / wall, "engines_built": self.engines_built}
+                 "spring_updates_per_s": springs_done / wall, "engines_built": self.engines_built,
+                 "max_concurrent": max_active}
         return records, stats
 
     def _collect_finished_quietly(self):
@@ -222,7 +231,7 @@ class RolloutServer:
         still = []
         finished, springs = False, 0
         for r, e, need, started, ns in active:
-            if not e.poll():
+            if not self._done(e):
                 still.append((r, e, need, started, ns))
                 continue
             pos = e.get_state(pos=True, vel=False)["pos"]
@@ -240,6 +249,12 @@ class RolloutServer:
         active[:] = still
         return finished, springs
 
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
     def close(self):
         for lst in self.pool.values():
             for e in lst:
@@ -248,3 +263,64 @@ class RolloutServer:
         for t in self.templates.values():
             t.close()
         self.templates.clear()
+
+
+class DeviceRolloutServer(RolloutServer):
+    """The same serving layer (arrival replay, HBM-budget admission, design
+    pooling, host-thread planning, latency records) over the device-resident
+    request loop (titan_gb300_server_*): rollouts are not launched on their
+    own streams but submitted to one persistent kernel, which admits them at
+    its next step boundary as slots free up, steps every active rollout's
+    tiles each step and reports finished ones through page-locked memory.
+    Every design runs the per-tile arithmetic with tiles of `tile` masses
+    (resident tiles off), so results are bit-identical to a rollout's own
+    step() with the per-tile kernel, alone or in any mix."""
+
+    def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_slots=4096, pool_per_design=64,
+                 tile=128, tile_smem_bytes=0):
+        super().__init__(precision, device, hbm_budget_bytes, max_active=max_slots, pool_per_design=pool_per_design,
+                         small_masses=0, resident_tiles=False)
+        self.tile = tile
+        self.server = Server(precision, device, max_slots, tile_smem_bytes)
+        self._ticket = {}  # engine id -> ticket
+
+    def _choice(self, n, ns):
+        return 1, self.tile
+
+    def _template(self, side, sc):
+        t = Sim(self.precision, self.device)
+        wl.load(t, sc, start=False, kernel=1, resident=(0, 0, 0))
+        return t
+
+    def _engine(self, side, sc):
+        if self.pool[side]:
+            return super()._engine(side, sc)
+        if side not in self.templates:
+            t = self._template(side, sc)
+            t.plan_host(self.tile)
+            self.templates[side] = t
+        e = Sim(self.precision, self.device)
+        wl.load(e, sc, start=False, kernel=1, resident=(0, 0, 0))
+        e.adopt_plan(self.templates[side])
+        e.start(self.tile)
+        self.engines_built += 1
+        if side not in self.bytes_of:
+            self.bytes_of[side] = float(e.device_bytes())
+        return e
+
+    def _launch(self, e, steps):
+        t = self.server.submit(e, steps)
+        if t is None:
+            raise RuntimeError("no free server slot (admission allows at most max_slots rollouts)")
+        self._ticket[id(e)] = t
+
+    def _done(self, e):
+        t = self._ticket.get(id(e))
+        if t is None or not self.server.poll(t):
+            return False
+        del self._ticket[id(e)]
+        return True
+
+    def close(self):
+        super().close()
+        self.server.close()
