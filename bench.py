@@ -73,6 +73,10 @@ def parse():
     p.add_argument("--serve-engine", default="device", choices=["device", "streams"],
                    help="device: the persistent request-server kernel; streams: one engine per request on its "
                         "own CUDA stream")
+    p.add_argument("--serve-stream-masses", type=int, default=20000,
+                   help="device engine: requests of at least this many masses run on their own stream (0: none)")
+    p.add_argument("--serve-prewarm", type=int, default=1,
+                   help="device engine: build the engines the requests need before the clock starts (1) or not (0)")
     p.add_argument("--serve-bodies", type=int, default=0,
                    help="instead of the rate sweep: this many single-body robot rollouts (3-12 masses per side, "
                         "5000 steps) submitted at once")
@@ -612,8 +616,9 @@ def run_serving(a, local):
     torch.cuda.set_device(local)
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
     if a.serve_engine == "device":
-        srv = serving.DeviceRolloutServer(prec, device=local)
-        engine = "device-resident request server (one persistent kernel, per-tile arithmetic, tiles of 128 masses)"
+        srv = serving.DeviceRolloutServer(prec, device=local, stream_masses=a.serve_stream_masses)
+        engine = ("device-resident request loop (one persistent kernel, per-tile arithmetic, tiles of 128 masses) "
+                  f"for requests under {a.serve_stream_masses} masses, own stream and automatic kernel above")
     else:
         srv = serving.RolloutServer(prec, device=local, small_masses=a.serve_small_masses)
         engine = "one engine per request on its own CUDA stream"
@@ -640,11 +645,28 @@ def run_serving(a, local):
         for r in reqs:
             warm.setdefault(r["side"], dict(r, arrival_s=0.0, steps=100))
     srv.run(list(warm.values()), scene_of=scene_of)
+    prewarmed = 0
+    if a.serve_engine == "device" and a.serve_prewarm:
+        # as many engines per design as any run has requests of it
+        counts = {}
+        for _, reqs in runs:
+            c = {}
+            for r in reqs:
+                c[r["side"]] = c.get(r["side"], 0) + 1
+            for side, k in c.items():
+                counts[side] = max(counts.get(side, 0), k)
+        by_side = {}
+        for r in warm.values():
+            by_side[r["side"]] = scene_of(r)
+        before = srv.engines_built
+        srv.prewarm(counts, lambda side: by_side[side])
+        prewarmed = srv.engines_built - before
     for rate, reqs in runs:
         recs, stats = srv.run(reqs, scene_of=scene_of)
         masses = sum(rec["masses"] for rec in recs.values())
         print(json.dumps({"workload": "rollout serving", "engine": engine, "requests": len(reqs),
-                          "rate_per_s": rate, "mean_masses": masses / len(recs), "precision": a.precision, **stats,
+                          "rate_per_s": rate, "mean_masses": masses / len(recs), "precision": a.precision,
+                          "engines_prebuilt": prewarmed, **stats,
                           "unit": UNIT}), flush=True)
     srv.close()
 

@@ -26,9 +26,9 @@
 // kBarrierNs, or host memory that stays silent past kIdleNs with no active
 // slot, ends the kernel with a status word the host reads; the host
 // relaunches it when it has work again.  A host-set stop word ends it at the
-// next step boundary.  Euler steps only; the CTA is the per-tile kernel's
-// launch-bound variant for two CTAs per SM, so that other kernels (the
-// scenes' transfers) keep room on each SM.
+// next step boundary.  Euler steps only; two 256-thread CTAs per SM with
+// the per-tile kernel's register-capped code (80 registers), so that other
+// kernels (the scenes' transfers) keep room on each SM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,6 +48,7 @@ namespace tg {
 namespace {
 
 constexpr int kServeThreads = 256;
+constexpr int kServeCtasPerSm = 2;  // registers capped for three: 2 x 256 x 80 leaves a fifth of the file
 constexpr int kRing = 16384;                     // ring entries (>= max slots)
 constexpr uint64_t kBarrierNs = 20000000000ull;  // 20 s
 constexpr uint64_t kIdleNs = 1000000000ull;      // 1 s without work: leave (the host relaunches)
@@ -230,7 +231,7 @@ __device__ void boundary(ServeSlot *slots, ServeCtl *ctl, int *active, int *pref
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(kServeThreads, 2)
+__global__ void __launch_bounds__(kServeThreads, 3)
     k_serve(ServeSlot *slots, ServeCtl *ctl, int *active, int *prefix, int *scratch, ServeHost *host,
             uint64_t *done, int max_slots) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(kServeThreads, 2)
             __syncthreads();
             const int local = s_local;
             const TileInfo ti = sa->tiles[local];
-            tile_step<PREC, 2, INTEG_EULER, true>(*sa, ti, tile_smem, s_parity, s_last, local == 0);
+            tile_step<PREC, 3, INTEG_EULER, true>(*sa, ti, tile_smem, s_parity, s_last, local == 0);
             __syncthreads();
         }
         if (!grid_sync(ctl)) {
@@ -393,7 +394,9 @@ int titan_gb300_server_create(titan_gb300_server **out, int device, int precisio
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, tg::kServeThreads, s->smem) != cudaSuccess ||
         per_sm < 1)
         return bail(TITAN_GB300_ELIMIT);
-    s->ctas = sms;  // one CTA per SM: the rest of each SM stays free for other kernels
+    // two CTAs per SM where they fit: the register cap and the tile budget
+    // leave each SM room for other kernels (the scenes' transfers)
+    s->ctas = sms * std::min(per_sm, tg::kServeCtasPerSm);
     if (cudaStreamCreateWithFlags(&s->run_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->ctl_stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(TITAN_GB300_ECUDA);
