@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--precision-study", action="store_true",
                    help="instead of the headline line: 64^3 lattice at dt=1e-5, FP32 and FP32C against FP64")
     p.add_argument("--study-steps", type=int, default=20000)
+    p.add_argument("--study-every", type=int, default=10000, help="steps between checkpoints of the precision study")
+    p.add_argument("--study-ref-steps", type=int, default=100000,
+                   help="steps of the reference's own CUDA kernels run beside the study's FP64 form")
     p.add_argument("--serving", action="store_true",
                    help="instead of the headline line: rollout serving, Poisson arrivals (p50/p99 latency)")
     p.add_argument("--serve-requests", type=int, default=400)
@@ -73,7 +76,7 @@ def parse():
     p.add_argument("--serve-engine", default="device", choices=["device", "streams"],
                    help="device: the persistent request-server kernel; streams: one engine per request on its "
                         "own CUDA stream")
-    p.add_argument("--serve-stream-masses", type=int, default=20000,
+    p.add_argument("--serve-stream-masses", type=int, default=0,
                    help="device engine: requests of at least this many masses run on their own stream (0: none)")
     p.add_argument("--serve-prewarm", type=int, default=1,
                    help="device engine: build the engines the requests need before the clock starts (1) or not (0)")
@@ -548,9 +551,16 @@ def run_suite(a, local):
 
 
 def run_precision_study(a, local):
-    """64^3 lattice dropped on a frictional plane, dt = 1e-5: FP32 and FP32C
-    trajectories against the FP64 form over --study-steps steps (a bounded
-    horizon of the 10^6-step study), plus total energy of each."""
+    """Long-horizon precision study: 64^3 lattice dropped on a frictional
+    plane, dt = 1e-5, --study-steps steps in FP64, FP32 and FP32C, a
+    checkpoint every --study-every steps: each mode's total energy and its
+    drift from the start, linear momentum, and FP32 / FP32C position error
+    against the FP64 form (the study's oracle, itself pinned to the CPU
+    oracle and to the reference's kernels by the tests); beside it, for the
+    first --study-ref-steps steps, the reference's own CUDA kernels from the
+    same start, whose distance from the FP64 form is the reference's own
+    run-to-run spread (float atomics).  One JSON line per checkpoint, then a
+    summary line."""
     import numpy as np
     import torch
 
@@ -560,43 +570,53 @@ def run_precision_study(a, local):
     torch.cuda.set_device(local)
     sc = wl.settling_lattice()
     n = sc["pos"].shape[0]
-    chunk = max(1, a.study_steps // 10)
     sims = {p: wl.make_sim(sc, p, 0, device=local) for p in (tg.FP64, tg.FP32, tg.FP32C)}
+    names = {tg.FP64: "f64", tg.FP32: "f32", tg.FP32C: "f32c"}
     g = float(abs(sc["g"][2]))
-    # the reference's own kernels (FP64, float atomics in scheduling order):
-    # their distance from the engine's FP64 trajectory is the spread the
-    # reference itself has between runs, the floor for any comparison
     from oracle import refgpu
-    ref = None if refgpu.available() else refgpu.RefGpuSim(sc, local)
+    ref = None
+    if a.study_ref_steps > 0 and refgpu.available() is None:
+        ref = refgpu.RefGpuSim(sc, local)
+    e0 = {p: float(s.diagnostics(g)["total"]) for p, s in sims.items()}
     rows = []
     done = 0
+    t0 = time.perf_counter()
     while done < a.study_steps:
-        k = min(chunk, a.study_steps - done)
+        k = min(a.study_every, a.study_steps - done)
         for s in sims.values():
             s.step(k)
         if ref is not None:
-            ref.step(k)
+            if done + k <= a.study_ref_steps:
+                ref.step(k)
+            else:
+                ref.close()
+                ref = None
         done += k
-        st = {p: s.get_state(pos=True, vel=True) for p, s in sims.items()}
+        st = {p: s.get_state(pos=True, vel=False) for p, s in sims.items()}
         row = {"steps": done, "t": done * sc["dt"]}
-        if ref is not None:
-            d = ref.state()["pos"] - st[tg.FP64]["pos"]
-            row["reference_kernels_max_pos_diff_m"] = float(np.max(np.abs(d)))
-            row["reference_kernels_rms_pos_diff_m"] = float(np.sqrt(np.mean(d * d)))
-        for p, key in ((tg.FP32, "f32"), (tg.FP32C, "f32c")):
-            d = st[p]["pos"] - st[tg.FP64]["pos"]
-            row[key + "_max_pos_err_m"] = float(np.max(np.abs(d)))
-            row[key + "_rms_pos_err_m"] = float(np.sqrt(np.mean(d * d)))
-        for p, key in ((tg.FP64, "f64"), (tg.FP32, "f32"), (tg.FP32C, "f32c")):
-            row[key + "_energy_j"] = float(sims[p].diagnostics(g)["total"])
+        for p, s in sims.items():
+            d = s.diagnostics(g)
+            row[names[p] + "_energy_j"] = float(d["total"])
+            row[names[p] + "_energy_drift_rel"] = (float(d["total"]) - e0[p]) / abs(e0[p])
+            row[names[p] + "_momentum"] = [float(x) for x in d["linear"]]
+        for p in (tg.FP32, tg.FP32C):
+            dd = st[p]["pos"] - st[tg.FP64]["pos"]
+            row[names[p] + "_max_pos_err_m"] = float(np.max(np.abs(dd)))
+            row[names[p] + "_rms_pos_err_m"] = float(np.sqrt(np.mean(dd * dd)))
+        if ref is not None and done <= a.study_ref_steps:
+            dr = ref.state()["pos"] - st[tg.FP64]["pos"]
+            row["reference_kernels_max_pos_diff_m"] = float(np.max(np.abs(dr)))
+            row["reference_kernels_rms_pos_diff_m"] = float(np.sqrt(np.mean(dr * dr)))
+        row["wall_s"] = time.perf_counter() - t0
         rows.append(row)
         print(json.dumps(row), flush=True)
     for s in sims.values():
         s.close()
     if ref is not None:
         ref.close()
-    print(json.dumps({"study": "64^3 lattice, dt=1e-5, plane mu 0.5", "masses": n, "steps": a.study_steps,
-                      "final": rows[-1]}), flush=True)
+    print(json.dumps({"study": "64^3 lattice dropped 0.05 m on a frictional plane (mu 0.5), damping 0.1, dt=1e-5",
+                      "masses": n, "steps": a.study_steps, "every": a.study_every,
+                      "reference_kernel_steps": min(a.study_ref_steps, a.study_steps), "final": rows[-1]}), flush=True)
 
 
 def run_serving(a, local):

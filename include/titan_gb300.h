@@ -240,7 +240,11 @@ int titan_gb300_step(titan_gb300_sim *sim, int64_t nsteps);
  * are dropped when the scene is rebuilt (integrator switch, topology change). */
 int titan_gb300_prepare_steps(titan_gb300_sim *sim, int64_t nsteps);
 
-/* Wait for queued work; replaces the cudaDeviceSynchronize at src/sim.cu:1570. */
+/* Wait for queued work; replaces the cudaDeviceSynchronize at src/sim.cu:1570.
+ * TITAN_GB300_ETIMEOUT from here, poll or wait (not wait's own time limit)
+ * means a step kernel's bounded wait for its shared-memory copies gave up:
+ * the kernel stopped early, so the scene's state is undefined and the
+ * handle must be destroyed. */
 int titan_gb300_synchronize(titan_gb300_sim *sim);
 
 /* step() is the asynchronous rollout launch.  poll(): TITAN_GB300_OK when

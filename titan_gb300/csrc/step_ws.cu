@@ -138,7 +138,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
                 ok = bounded_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
                 if (ok && lane == 0) *idx_waited = k + 1;
             }
-            if (__any_sync(0xffffffffu, !ok)) {
+            // a consumer group that gave up raised the abort word: no copy is
+            // issued after that, so the drain below waits only for copies
+            // that are certain to complete
+            if (__any_sync(0xffffffffu, !ok || *abort_word)) {
                 if (lane == 0) {
                     *abort_word = 1;
                     atomicOr(a.err, 1);

@@ -285,12 +285,15 @@ class DeviceRolloutServer(RolloutServer):
     per-tile arithmetic with tiles of `tile` masses (resident tiles off), so
     results are bit-identical to a rollout's own step() with the per-tile
     kernel, alone or in any mix.  Rollouts of at least stream_masses masses
-    (0: none) run on their own engine and stream with the automatic kernel,
-    where a large scene steps fastest (measured on GB300, 100^3 lattice:
-    0.121 ms per step there against 0.336 ms in the request loop)."""
+    (0, the default: none) run on their own engine and stream with the
+    automatic kernel, where a large scene steps fastest (measured on GB300,
+    100^3 lattice: 0.121 ms per step there against 0.336 ms in the request
+    loop) -- but that kernel takes a whole SM's shared memory, so it runs
+    only while the request loop's kernel is not resident (it leaves one
+    second after its last rollout): mixing the two serialises them."""
 
     def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_slots=4096, pool_per_design=4096,
-                 tile=128, tile_smem_bytes=0, stream_masses=20000):
+                 tile=128, tile_smem_bytes=0, stream_masses=0):
         super().__init__(precision, device, hbm_budget_bytes, max_active=max_slots, pool_per_design=pool_per_design,
                          small_masses=0, resident_tiles=True)
         self.tile = tile
