@@ -178,12 +178,18 @@ int titan_gb300_set_launch(titan_gb300_sim *sim, int threads_per_cta);
  * CTA is larger than 256 threads.  Used by the autotuner. */
 int titan_gb300_set_occupancy(titan_gb300_sim *sim, int min_ctas_per_sm);
 
-/* Step kernel form: 0 = automatic (currently the per-tile kernel, the faster
- * form measured on GB300), 1 = per-tile kernel (one CTA per tile), 2 =
- * pipelined persistent kernel (TMA-staged tiles; fails at start() when two
- * tiles do not fit in shared memory), 3 = per-tile kernel whose slab records
- * and tile states arrive by bulk copy (TMA) and halo by cp.async, all issued
- * before one wait.  All forms give bit-identical results.  Set before
+/* Step kernel form (extension; the reference has one pair of kernels):
+ * 0 = automatic: the warp-specialised kernel in FP32 and FP32C (measured
+ * fastest on GB300), the per-tile kernel in FP64, and resident tiles for
+ * halo-free tiles (set_resident); 1 = per-tile kernel (one CTA per tile);
+ * 3 = per-tile kernel whose slab records and tile states arrive by bulk
+ * copy (TMA) and halo by cp.async, all issued before one wait; 4 =
+ * warp-specialised persistent kernel (a producer warp streams tiles into a
+ * shared-memory ring, two consumer groups compute; fails at start() when two
+ * tiles do not fit); 6 = pull kernel, FP32 and FP32C only (every mass sums
+ * its own springs' forces from streamed spring columns against tile states
+ * a producer warp stages; fails at start() in FP64 or with a mass above the
+ * heavy threshold).  All forms give bit-identical results.  Set before
  * start(). */
 int titan_gb300_set_kernel(titan_gb300_sim *sim, int variant);
 
