@@ -893,7 +893,7 @@ int build_device(titan_gb300_sim *s) {
         CK(cudaGetDevice(&dev), "device");
         CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device");
         s->ctas = (int)std::min<int64_t>((int64_t)tiles_run.size(), sms);
-        s->threads = (s->ws_warps + 1) * 32;
+        s->threads = (s->ws_warps + tg::kWsProducerWarps) * 32;
         s->use_ws = true;
     }
     if (s->use_pull) {

@@ -53,7 +53,8 @@ struct WsLayout {
     int32_t tinfo, params, mbar, total;       // per-stage TileInfo, DevParams copy, barriers
 };
 constexpr int kWsMaxStages = 3;
-constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7, + the producer warp: 480 threads
+constexpr int kWsMaxConsumerWarps = 14;  // two groups of 7
+constexpr int kWsProducerWarps = 2;      // share each tile's halo gathers: 512 threads in all
 
 // Shared-memory layout of the pull kernel (step_pull.cu): nstages stages of
 // one tile's state records (tile masses, then halo) and its actuation

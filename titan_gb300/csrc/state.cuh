@@ -40,6 +40,8 @@ __device__ __forceinline__ St<PREC> load_state(const void *buf, int64_t g) {
         float2 a1 = __ldg(reinterpret_cast<const float2 *>(p + 1));
         s.x[0] = a0.x; s.x[1] = a0.y; s.x[2] = a0.z;
         s.v[0] = a0.w; s.v[1] = a1.x; s.v[2] = a1.y;
+        s.xl[0] = s.xl[1] = s.xl[2] = 0.f;  // the epilogue adds the (zero) low parts
+        s.vl[0] = s.vl[1] = s.vl[2] = 0.f;
     }
     return s;
 }

@@ -5,13 +5,16 @@
 // alternate, inside each CTA, between waiting for a tile's data and
 // computing on it; here the two run concurrently in one persistent CTA per
 // SM:
-//   * the producer warp walks the CTA's tiles (b, b + G, b + 2G, ...) and,
-//     for each, waits until a stage of the shared-memory ring is free, then
-//     streams the tile into it: the slab records (into the force slots) and
-//     the tile masses' state records as bulk copies on the Tensor Memory
-//     Accelerator, and the halo state records as 16-byte cp.async gathers by
-//     the warp's 32 lanes, all counted on the stage's "full" mbarrier (one
-//     expect-tx arrival plus one cp.async arrival per lane).  The halo index
+//   * two producer warps walk the CTA's tiles (b, b + G, b + 2G, ...) and,
+//     for each, wait until a stage of the shared-memory ring is free, then
+//     stream the tile into it: the first issues the slab records (into the
+//     force slots) and the tile masses' state records as bulk copies on the
+//     Tensor Memory Accelerator, and both gather the halo state records as
+//     16-byte cp.async copies, all counted on the stage's "full" mbarrier
+//     (one expect-tx arrival plus one cp.async arrival per producer lane).
+//     The halo gathers are what a consumer group waits for once its stage
+//     is free, so two warps share them (one takes about 2,700 cycles per
+//     tile of 208 masses).  The halo index
 //     list of the next tile arrives by bulk copy into a two-entry ring while
 //     the current tile is issued, so no gather waits on an index load;
 //     The stage also receives the tile's actuation records and incidence
@@ -41,7 +44,9 @@ namespace tg {
 namespace {
 
 constexpr int kBatchB = 3;  // slab entries per thread in flight (phase B); 4 spills at the 128-register cap
-constexpr int kWsThreads = (kWsMaxConsumerWarps + 1) * 32;
+constexpr int kWsThreads = (kWsMaxConsumerWarps + kWsProducerWarps) * 32;
+constexpr int kProdThreads = kWsProducerWarps * 32;
+constexpr int kProdBar = 3;  // named barrier of the producer warps (the groups use 1 and 2)
 
 template <int PREC>
 __host__ __device__ constexpr int ws_rec() { return PREC == P_FP32 ? 32 : 48; }
@@ -88,7 +93,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
     // leave, and everything it does before its grid_dep_wait() reads only
     // data no step writes (see the producer and the consumers below)
     grid_dep_launch_dependents();
-    const int ncw = (int)(blockDim.x >> 5) - 1;  // consumer warps (even)
+    const int ncw = (int)(blockDim.x >> 5) - kWsProducerWarps;  // consumer warps (even)
     const int gw = ncw >> 1;                     // warps per group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int G = gridDim.x;
@@ -96,7 +101,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; s++) {
-            mbar_init(&full[s], 33);  // expect-tx arrival + one cp.async arrival per producer lane
+            mbar_init(&full[s], 1 + kProdThreads);  // expect-tx arrival + one cp.async arrival per producer lane
             mbar_init(&empty[s], (uint32_t)gw);
         }
         mbar_init(&idxbar[0], 1);
@@ -110,9 +115,13 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
     }
     __syncthreads();
 
-    if (warp == ncw) {
-        // ---------------- producer warp ----------------
+    if (warp >= ncw) {
+        // ---------------- producer warps ----------------
+        // warp ncw issues the bulk copies and the index lists; every
+        // producer warp gathers its share of each tile's halo records
         constexpr int kChunks = kRec / 16;
+        const bool lead = warp == ncw && lane == 0;
+        const int pl = threadIdx.x - ncw * 32;  // lane among the producer warps
         // halo indices of tile j go to ring entry j & 1 (lists are padded to
         // a multiple of 4 entries, so each copy is a multiple of 16 bytes)
         auto issue_idx = [&](int j, const TileInfo &tj) {
@@ -125,7 +134,7 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
         };
         TileInfo ti = {};
         if (blockIdx.x < ntiles) ti = a.tiles[blockIdx.x];
-        if (lane == 0 && blockIdx.x < ntiles) issue_idx(0, ti);
+        if (lead && blockIdx.x < ntiles) issue_idx(0, ti);
         int k = 0;
         for (int t = blockIdx.x; t < ntiles; t += G, k++) {
             const int s = k % NS;
@@ -136,20 +145,20 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
             bool ok = bounded_wait(&empty[s], ph ^ 1u, abort_word, 200);
             if (ok) {
                 ok = bounded_wait(&idxbar[k & 1], (uint32_t)(k >> 1) & 1u, abort_word);
-                if (ok && lane == 0) *idx_waited = k + 1;
+                if (ok && lead) *idx_waited = k + 1;
             }
             // a consumer group that gave up raised the abort word: no copy is
             // issued after that, so the drain below waits only for copies
-            // that are certain to complete
-            if (__any_sync(0xffffffffu, !ok || *abort_word)) {
-                if (lane == 0) {
+            // that are certain to complete (the producer warps decide as one)
+            if (group_any(kProdBar, kProdThreads, !ok || *abort_word)) {
+                if (lead) {
                     *abort_word = 1;
                     atomicOr(a.err, 1);
                 }
                 break;
             }
             uint8_t *st = smem + (int64_t)s * L.stage;
-            if (lane == 0) {
+            if (lead) {
                 tinfo[s] = ti;  // published by the arrival below
                 fence_proxy_async();
                 const uint32_t eb = (uint32_t)ti.ne * kSlot, ab = (uint32_t)ti.nact * kSlot;
@@ -167,19 +176,19 @@ __global__ void __launch_bounds__(kWsThreads, 1) k_step_ws(StepArgs a, int parit
             // slab, actuation, incidence and halo-index blocks are constant
             // across steps; the state records are the previous step's output
             if (k == 0) grid_dep_wait();
-            if (lane == 0) issue_chunks(st, in + (int64_t)ti.mass_off * kRec, (uint32_t)ti.nm * kRec, &full[s]);
-            // halo records, one per lane at a time (the producer issues for
-            // every stage: its instruction count is on the critical path)
+            if (lead) issue_chunks(st, in + (int64_t)ti.mass_off * kRec, (uint32_t)ti.nm * kRec, &full[s]);
+            // halo records, one per producer lane at a time (their issue is
+            // on the critical path)
             const int32_t *ix = idxbuf + (k & 1) * L.idx_words;
-            for (int h = lane; h < ti.nh; h += 32) {
+            for (int h = pl; h < ti.nh; h += kProdThreads) {
                 const uint8_t *src = in + (int64_t)ix[h] * kRec;
                 uint8_t *dst = st + (int64_t)(ti.nm + h) * kRec;
 #pragma unroll
                 for (int c = 0; c < kChunks; c++) cp_async16(dst + 16 * c, src + 16 * c);
             }
             cp_async_arrive(&full[s]);
-            __syncwarp();  // every lane has read ring entry k & 1
-            if (lane == 0) {
+            group_sync(kProdBar, kProdThreads);  // every producer lane has read ring entry k & 1
+            if (lead) {
                 *issued_word = k + 1;
                 if (has_next) issue_idx(k + 1, tn);
             }
@@ -336,7 +345,7 @@ cudaError_t launch_step_ws(int precision, int integ, const StepArgs &a, int ctas
     // programmatic stream serialisation: the next step's grid may start
     // while this one drains (the kernel orders its dependent reads itself)
     void *args[] = {const_cast<StepArgs *>(&a), &parity, &write_acc};
-    return launch_programmatic(ws_kernel(precision, integ), dim3(ctas), dim3((consumer_warps + 1) * 32), args,
+    return launch_programmatic(ws_kernel(precision, integ), dim3(ctas), dim3((consumer_warps + kWsProducerWarps) * 32), args,
                                (size_t)a.ws.total, s);
 }
 
