@@ -1924,7 +1924,9 @@ int titan_gb300_set_mass_state(titan_gb300_sim *s, int64_t count, const int64_t 
         Tcur.resize(s->n);
         mass_times(s, nullptr, s->n, Tcur.data());
     }
-    for (int64_t q = 0; q < count; q++) {
+    // per-mass host bookkeeping, only for the attributes given (a loop over
+    // every mass costs milliseconds on a million-mass scene)
+    for (int64_t q = 0; (m || ext || drag || T || fixed) && q < count; q++) {
         int64_t i = idx ? idx[q] : q;
         if (m) s->m[i] = m[q];
         if (ext) {
