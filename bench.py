@@ -637,7 +637,7 @@ def run_serving(a, local):
     prec = {"f32c": tg.FP32C, "f64": tg.FP64, "f32": tg.FP32}[a.precision]
     if a.serve_engine == "device":
         srv = serving.DeviceRolloutServer(prec, device=local, stream_masses=a.serve_stream_masses)
-        engine = "device-resident request loop (one persistent kernel, per-tile arithmetic, tiles of 128 masses)"
+        engine = f"device-resident request loop (one persistent kernel, per-tile arithmetic, tiles of {srv.tile} masses)"
         engine += (f" for requests under {a.serve_stream_masses} masses, own stream and automatic kernel above"
                    if a.serve_stream_masses > 0 else " for every request")
     else:

@@ -365,7 +365,7 @@ int titan_gb300_diagnostics_noalloc(const double *pos, const double *vel, const 
  * leaves after a second without work and is launched again by the next
  * submit or poll; every wait in it is bounded.
  *   create: max_slots scenes at once (1 to 16384); tile_smem_bytes of
- *     shared memory for one tile (0: 96 KiB; scenes whose tiles need more
+ *     shared memory for one tile (0: 112,000 bytes; scenes whose tiles need more
  *     are refused -- plan them with smaller tiles).
  *   submit: the scene must be started (start()) on the server's device and
  *     precision, with symplectic Euler and resident tiles and bins off

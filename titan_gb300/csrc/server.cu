@@ -48,6 +48,7 @@ namespace tg {
 namespace {
 
 constexpr int kServeThreads = 256;
+constexpr size_t kServeTileSmem = 112000;  // default shared memory for one tile
 constexpr int kServeCtasPerSm = 2;  // registers capped for three: 2 x 256 x 80 leaves a fifth of the file
 constexpr int kRing = 16384;                     // ring entries (>= max slots)
 constexpr uint64_t kBarrierNs = 20000000000ull;  // 20 s
@@ -382,7 +383,10 @@ int titan_gb300_server_create(titan_gb300_server **out, int device, int precisio
     s->device = device;
     s->prec = precision;
     s->max_slots = max_slots;
-    s->tile_smem = tile_smem_bytes > 0 ? (size_t)tile_smem_bytes : 96 * 1024;
+    // default: room for a 208-mass FP32C tile of a lattice (about 103 KB of
+    // records) while two CTAs, each with its launch parameters, still share
+    // one SM (2 x 112,352 bytes)
+    s->tile_smem = tile_smem_bytes > 0 ? (size_t)tile_smem_bytes : kServeTileSmem;
     s->smem = ((sizeof(tg::StepArgs) + 15) & ~size_t(15)) + s->tile_smem;
     if (cudaSetDevice(device) != cudaSuccess) return bail(TITAN_GB300_ECUDA);
     const void *f = tg::serve_kernel(precision);

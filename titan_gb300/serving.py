@@ -293,10 +293,13 @@ class DeviceRolloutServer(RolloutServer):
     second after its last rollout): mixing the two serialises them."""
 
     def __init__(self, precision=FP32C, device=0, hbm_budget_bytes=120e9, max_slots=4096, pool_per_design=4096,
-                 tile=128, tile_smem_bytes=0, stream_masses=0):
+                 tile=None, tile_smem_bytes=0, stream_masses=0):
         super().__init__(precision, device, hbm_budget_bytes, max_active=max_slots, pool_per_design=pool_per_design,
                          small_masses=0, resident_tiles=True)
-        self.tile = tile
+        # tiles of 208 masses fit the loop's default tile memory in FP32 and
+        # FP32C (0.305 ms per 100^3 step against 0.331 with 128); FP64
+        # records are larger
+        self.tile = tile if tile is not None else (128 if precision == FP64 else 208)
         self.stream_masses = stream_masses
         self.server = Server(precision, device, max_slots, tile_smem_bytes)
         self._ticket = {}  # id(engine) -> ticket (request-loop rollouts)
