@@ -386,7 +386,7 @@ int titan_gb300_server_create(titan_gb300_server **out, int device, int precisio
     // default: room for a 208-mass FP32C tile of a lattice (about 103 KB of
     // records) while two CTAs, each with its launch parameters, still share
     // one SM (2 x 112,352 bytes)
-    s->tile_smem = tile_smem_bytes > 0 ? (size_t)tile_smem_bytes : kServeTileSmem;
+    s->tile_smem = tile_smem_bytes > 0 ? (size_t)tile_smem_bytes : tg::kServeTileSmem;
     s->smem = ((sizeof(tg::StepArgs) + 15) & ~size_t(15)) + s->tile_smem;
     if (cudaSetDevice(device) != cudaSuccess) return bail(TITAN_GB300_ECUDA);
     const void *f = tg::serve_kernel(precision);
