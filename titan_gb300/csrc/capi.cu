@@ -1087,12 +1087,18 @@ cudaGraphExec_t get_graph(titan_gb300_sim *s, int len, int parity, cudaError_t &
     e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return nullptr;
     int p = parity;
+    cudaError_t el = cudaSuccess;  // the first launch refused while capturing
     for (int i = 0; i < len; i++)
         for (int q = 0; q < s->passes(); q++) {
-            s->launch(p, 0, q);
+            const cudaError_t r = s->launch(p, 0, q);
+            if (el == cudaSuccess) el = r;
             p ^= 1;
         }
     e = cudaStreamEndCapture(s->stream, &g);
+    if (e == cudaSuccess && el != cudaSuccess) {
+        cudaGraphDestroy(g);
+        e = el;
+    }
     if (e != cudaSuccess) return nullptr;
     cudaGraphExec_t ex = nullptr;
     e = cudaGraphInstantiate(&ex, g, 0);
