@@ -72,12 +72,14 @@ def test_small_designs_run_as_one_resident_tile():
     srv.close()
 
 
-def test_device_server_result_is_the_same_alone_and_in_a_mix():
-    """The same through the device-resident request loop: every request of a
-    Poisson stream (designs of 27 to 1000 masses, horizons 100 to 600 steps)
-    gives the bits it gives alone."""
+@pytest.mark.parametrize("precision", [tg.FP32C, tg.FP64])
+def test_device_server_result_is_the_same_alone_and_in_a_mix(precision):
+    """The same through the device-resident request loop (its default tiles:
+    208 masses in FP32C, 128 in FP64): every request of a Poisson stream
+    (designs of 27 to 1000 masses, horizons 100 to 600 steps) gives the bits
+    it gives alone, and the bits of its own step() with other tiles."""
     reqs = wl.request_stream(24, 400.0, seed=8, mass_range=(27, 1000), horizon=(100, 600))
-    with serving.DeviceRolloutServer(tg.FP32C) as srv:
+    with serving.DeviceRolloutServer(precision) as srv:
         alone = {}
         for r in reqs[:5]:
             recs, _ = srv.run([dict(r, arrival_s=0.0)], keep_results=True)
@@ -87,7 +89,7 @@ def test_device_server_result_is_the_same_alone_and_in_a_mix():
     for rid, pos in alone.items():
         assert np.array_equal(recs[rid]["pos"], pos), rid
     for r in reqs:
-        s = wl.make_sim(wl.rollout_request(r["side"], r["seed"]), tg.FP32C, 128, kernel=1, resident=(0, 0, 0))
+        s = wl.make_sim(wl.rollout_request(r["side"], r["seed"]), precision, 96, kernel=1, resident=(0, 0, 0))
         s.step(r["steps"])
         assert np.array_equal(recs[r["id"]]["pos"], s.get_state(pos=True, vel=False)["pos"]), r["id"]
         s.close()
